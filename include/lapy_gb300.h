@@ -1,0 +1,225 @@
+/*
+ * lapy_gb300 — C ABI of the GB300 (sm_103a) linear-FEM Laplace–Beltrami path.
+ *
+ * Every entry point takes plain device pointers, sizes and a cudaStream_t
+ * (passed as void*), returns an int status (LAPY_OK == 0, negative on error)
+ * and never throws.  No function allocates device memory: buffers, including
+ * scratch ("workspace"), are allocated by the caller, whose size the matching
+ * *_workspace_bytes() query returns.  Indices are int32, matrix values f64
+ * unless the name says f32.
+ *
+ * The reference (Deep-MI/LaPy) is pure Python over SciPy; it has no FFI.
+ * Each entry point below names the reference function whose work it performs;
+ * the Python package lapy_gb300 binds them with ctypes and mirrors the
+ * reference's Python API (Solver, heat.diffusion, diffgeo, shapedna).
+ */
+#ifndef LAPY_GB300_H
+#define LAPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LAPY_OK 0
+#define LAPY_ERR_INVALID (-1)   /* bad argument (size, pointer, alignment)   */
+#define LAPY_ERR_CUDA (-2)      /* CUDA runtime error                        */
+#define LAPY_ERR_NOCONV (-3)    /* iteration cap reached before tolerance    */
+#define LAPY_ERR_BREAKDOWN (-4) /* Krylov breakdown (p'Ap <= 0, rank loss)   */
+#define LAPY_ERR_NAN (-5)       /* NaN/Inf met in the iteration              */
+#define LAPY_ERR_TIMEOUT (-6)   /* a bounded device-side wait gave up        */
+#define LAPY_ERR_WORKSPACE (-7) /* workspace smaller than the query result   */
+#define LAPY_ERR_PATTERN (-8)   /* matrix pattern not contained in A's       */
+
+/* Library version (major*10000 + minor*100 + patch). */
+int lapy_version(void);
+/* Human-readable text for a status code. */
+const char* lapy_status_string(int status);
+/* Detail text of the last error recorded by this thread ("" if none). */
+const char* lapy_last_error(void);
+/* Kernel launches issued by this library since it was loaded. */
+long long lapy_launch_count(void);
+/* PCG profile: when enabled, every persistent PCG launch is timed with CUDA
+ * events and its work counted.  lapy_profile_read fills up to n of
+ * {pcg_ms, pcg_launches, pcg_iterations, rows_processed, nnz_processed,
+ *  algorithmic_bytes}. */
+void lapy_profile_enable(int on);
+void lapy_profile_reset(void);
+int lapy_profile_read(double* out, int n);
+
+/* ---- FEM assembly: symbolic CSR build ----------------------------------
+ * Replaces the COO -> CSC duplicate summation of
+ *   lapy/solver.py:171-178 (_fem_tria), :286-293 (_fem_tria_aniso),
+ *   :472-501 (_fem_tetra)
+ * i.e. scipy.sparse.csc_matrix((data, (i, j))).  The element connectivity
+ * `elems` (m x npe, npe = 3 or 4, row-major int32) yields the local (i, j)
+ * pairs in the reference's order; the CSR pattern of the n x n result is the
+ * set of distinct pairs, rows ascending, columns ascending inside a row
+ * (A is symmetric, so these arrays equal the reference's CSC arrays).
+ *
+ * Two calls, because nnz is only known after the first:
+ *   lapy_csr_symbolic_count  -> indptr (n+1, device) and *nnz_out (host)
+ *   lapy_csr_symbolic_fill   -> indices (nnz), seg_ptr (nnz+1), seg_src (m*L)
+ * seg_src lists the local-entry positions (e*L + l, L = npe*npe) sorted by
+ * (row, col, position); seg_ptr[k]..seg_ptr[k+1] is the run summed into
+ * nonzero k.  The numeric kernels below use (seg_ptr, seg_src).
+ */
+size_t lapy_csr_symbolic_workspace_bytes(int64_t n, int64_t m, int npe);
+int lapy_csr_symbolic_count(const int32_t* elems, int64_t m, int npe, int64_t n,
+                            int32_t* indptr, int64_t* nnz_out, void* workspace,
+                            size_t ws_bytes, void* stream);
+int lapy_csr_symbolic_fill(const int32_t* elems, int64_t m, int npe, int64_t n,
+                           const int32_t* indptr, int64_t nnz, int32_t* indices,
+                           int32_t* seg_ptr, int32_t* seg_src, void* workspace,
+                           size_t ws_bytes, void* stream);
+
+/* ---- FEM assembly: numeric ---------------------------------------------
+ * Element math in the coordinate type (coords_f32 != 0: float32 coordinates,
+ * as the reference's mesh readers produce; else float64), then summed per
+ * nonzero in (element, local) order into out_f32 ? float32 : float64 values.
+ *
+ * lapy_fem_tria_numeric    <- lapy/solver.py:105-194  (_fem_tria)
+ * lapy_fem_tria_aniso_numeric <- lapy/solver.py:196-308 (_fem_tria_aniso);
+ *      u1, u2: m x 3 float64 curvature frame, aniso_mat: m x 2 float64
+ *      (tria_mesh.py:1221-1279 and solver.py:88-90 produce them on the host)
+ * lapy_fem_tet_numeric     <- lapy/solver.py:379-533  (_fem_tetra)
+ *
+ * a_vals, m_vals: nnz values of A and M on the pattern from the symbolic
+ * step.  lump != 0: m_vals instead receives n diagonal values (the lumped
+ * mass, solver.py:188-193 / :527-532).  `work` must hold
+ * lapy_fem_numeric_workspace_bytes(m, npe) bytes.
+ */
+size_t lapy_fem_numeric_workspace_bytes(int64_t m, int npe);
+int lapy_fem_tria_numeric(const void* v, int coords_f32, const int32_t* t, int64_t m,
+                          int64_t n, const int32_t* indptr, const int32_t* indices,
+                          const int32_t* seg_ptr, const int32_t* seg_src, int64_t nnz,
+                          int lump, int out_f32, void* a_vals, void* m_vals, void* work,
+                          size_t ws_bytes, void* stream);
+int lapy_fem_tria_aniso_numeric(const void* v, int coords_f32, const int32_t* t,
+                                int64_t m, const double* u1, const double* u2,
+                                const double* aniso_mat, int64_t n, const int32_t* indptr,
+                                const int32_t* indices, const int32_t* seg_ptr,
+                                const int32_t* seg_src, int64_t nnz, int lump, int out_f32,
+                                void* a_vals, void* m_vals, void* work, size_t ws_bytes,
+                                void* stream);
+int lapy_fem_tet_numeric(const void* v, int coords_f32, const int32_t* t, int64_t m,
+                         int64_t n, const int32_t* indptr, const int32_t* indices,
+                         const int32_t* seg_ptr, const int32_t* seg_src, int64_t nnz,
+                         int lump, int out_f32, void* a_vals, void* m_vals, void* work,
+                         size_t ws_bytes, void* stream);
+
+/* Position of the diagonal entry of every row (-1 if absent). */
+int lapy_csr_diag_index(int64_t n, const int32_t* indptr, const int32_t* indices,
+                        int32_t* diag_pos, void* stream);
+
+/* Map the pattern (b_indptr, b_indices) into A's pattern: pos[k] = index in A
+ * of B's nonzero k.  Returns LAPY_ERR_PATTERN if some entry is not in A.
+ * `work`: >= 256 bytes of device scratch.  Used when a caller replaces
+ * Solver.mass (lapy/diffgeo.py:149 sets it to the identity). */
+int lapy_csr_pattern_map(int64_t n, const int32_t* a_indptr, const int32_t* a_indices,
+                         const int32_t* b_indptr, const int32_t* b_indices,
+                         int64_t b_nnz, int32_t* pos, void* work, void* stream);
+
+/* Mean edge length over the strict upper triangle of the pattern
+ * (lapy/tria_mesh.py:735-748, lapy/tet_mesh.py:182-195: the mean of
+ * ||v_i - v_j|| over the distinct edges).  Result written to *out (host). */
+int lapy_avg_edge_length(const void* v, int coords_f32, int64_t n, const int32_t* indptr,
+                         const int32_t* indices, double* out, void* work,
+                         size_t ws_bytes, void* stream);
+size_t lapy_avg_edge_length_workspace_bytes(int64_t n);
+
+/* ---- sparse matrix-vector products -------------------------------------
+ * Y = alpha * Mat * X + beta * Y for X, Y row-major n x ncol.  Used wherever
+ * the reference multiplies by A or M (solver.py:844-846, heat.py:208 ...).
+ * group: lanes per row (4, 8, 16 or 32; 0 = autotuned choice). */
+int lapy_csr_spmm_f64(int64_t n, const int32_t* indptr, const int32_t* indices,
+                      const double* vals, int ncol, const double* x, double* y,
+                      double alpha, double beta, int group, void* stream);
+int lapy_csr_spmm_f32(int64_t n, const int32_t* indptr, const int32_t* indices,
+                      const float* vals, int ncol, const float* x, float* y,
+                      float alpha, float beta, int group, void* stream);
+/* Diagonal-matrix variant Y = alpha * diag(d) X + beta * Y. */
+int lapy_diag_mm_f64(int64_t n, const double* d, int ncol, const double* x, double* y,
+                     double alpha, double beta, void* stream);
+
+/* ---- element-wise helpers ----------------------------------------------
+ * out = a*x + b*y (y may be NULL).  Forms hmat = M + t*A (lapy/heat.py:208)
+ * and A - sigma*M (lapy/solver.py:707) on a shared pattern. */
+int lapy_vec_axpby(int64_t n, double a, const double* x, double b, const double* y,
+                   double* out, void* stream);
+/* vals[diag_pos[i]] += b * d[i]: adds a lumped (diagonal) mass to a matrix. */
+int lapy_csr_add_diag(int64_t n, const int32_t* diag_pos, double b, const double* d,
+                      double* vals, void* stream);
+/* Dirichlet masking (lapy/solver.py:847-865): rows and columns of masked
+ * vertices become identity rows, so the masked system equals the reduced
+ * system A[free][:, free] of the reference.  dmask: n bytes, 1 = Dirichlet. */
+int lapy_csr_dirichlet_mask(int64_t n, const int32_t* indptr, const int32_t* indices,
+                            const double* vals, const uint8_t* dmask, double* out_vals,
+                            void* stream);
+
+/* ---- linear solves -------------------------------------------------------
+ * Replaces splu(K).solve(B) of lapy/solver.py:873-877 (Poisson) and
+ * lapy/heat.py:223-227 (heat).  K (n x n CSR, f64) is block diagonal over
+ * `nseg` segments (seg_row: host array, nseg+1 row offsets); B and X are
+ * row-major n x ncol.  mixed != 0: FP32 Jacobi-PCG inside FP64 iterative
+ * refinement (each round to inner_rtol); mixed == 0: FP64 Jacobi-PCG.
+ * Stops when ||B - K X|| <= rtol ||B|| per (segment, column).
+ * status_out / relres_out: host arrays nseg*ncol (row s*ncol + c). */
+size_t lapy_pcg_solve_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row,
+                                      int ncol, int mixed);
+int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices,
+                   const double* k_vals, int64_t nnz, int nseg, const int32_t* seg_row,
+                   int ncol, const double* b, double* x, double rtol, int maxiter, int mixed,
+                   double inner_rtol, int32_t* status_out, double* relres_out,
+                   int64_t* iters_out, void* ws, size_t ws_bytes, void* stream);
+
+/* ---- generalized eigenproblem -------------------------------------------
+ * Replaces Solver.eigs (lapy/solver.py:667-716): the k eigenpairs of
+ * A x = lambda M x nearest sigma, by block shift-invert Lanczos (block width
+ * `block` in {1,2,4,8,16}) on (A - sigma M)^-1 M in the M inner product, for
+ * every segment of a block-diagonal batch at once.  M is given on A's pattern
+ * (m_is_diag == 0, nnz values) or as its diagonal (m_is_diag != 0, n values).
+ * evals: device nseg*k (ascending per segment); evecs: device row-major n x k,
+ * M-orthonormal per segment.  status_out / nbasis_out: host nseg.
+ * tol: Ritz residual tolerance; inner_rtol: inner-solve residual target. */
+size_t lapy_eigs_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row,
+                                 int k, int block, int max_vectors);
+int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const int32_t* indices,
+                           const double* a_vals, const double* m_vals, int m_is_diag,
+                           int64_t nnz, int nseg, const int32_t* seg_row, double sigma, int k,
+                           int block, int max_vectors, double tol, double inner_rtol,
+                           int inner_maxiter, uint64_t seed, double* evals, double* evecs,
+                           int32_t* status_out, int32_t* nbasis_out, int64_t* inner_iters_out,
+                           void* ws, size_t ws_bytes, void* stream);
+
+/* ---- heat-method geodesics (lapy/diffgeo.py) ----------------------------
+ * Gradient per element of nf vertex functions f (row-major n x nf) into
+ * out (m x nf x 3): tria_compute_gradient (diffgeo.py:222-300) and
+ * tet_compute_gradient (diffgeo.py:846-922). */
+int lapy_tria_gradient(const void* v, int coords_f32, const int32_t* t, int64_t m,
+                       const double* f, int nf, double* out, void* stream);
+int lapy_tet_gradient(const void* v, int coords_f32, const int32_t* t, int64_t m,
+                      const double* f, int nf, double* out, void* stream);
+/* In-place g / ||g|| of `rows` 3-vectors, zero vectors -> 0
+ * (diffgeo.py:153-154, the nan_to_num normalisation). */
+int lapy_normalize_rows3(int64_t rows, int reserved, double* g, void* stream);
+/* Integrated divergence at vertices (diffgeo.py:303-387 and :925-1006) of
+ * tfunc (m x nf x 3); the vertex sums walk the assembly map's diagonal runs
+ * (diag_pos from lapy_csr_diag_index, seg_ptr/seg_src from the symbolic
+ * step).  work: m * npe * nf doubles. */
+int lapy_tria_divergence(const void* v, int coords_f32, const int32_t* t, int64_t m,
+                         int64_t n, const int32_t* diag_pos, const int32_t* seg_ptr,
+                         const int32_t* seg_src, const double* tfunc, int nf, double* out,
+                         double* work, void* stream);
+int lapy_tet_divergence(const void* v, int coords_f32, const int32_t* t, int64_t m,
+                        int64_t n, const int32_t* diag_pos, const int32_t* seg_ptr,
+                        const int32_t* seg_src, const double* tfunc, int nf, double* out,
+                        double* work, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LAPY_GB300_H */

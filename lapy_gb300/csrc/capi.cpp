@@ -1,0 +1,98 @@
+// Library-level C ABI: version, status strings, per-thread last-error text.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <atomic>
+#include <mutex>
+#include <vector>
+#include "lapy_gb300.h"
+
+static thread_local char g_last_error[512] = {0};
+
+void lapy_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+  snprintf(g_last_error, sizeof(g_last_error), "CUDA error %d (%s) in %s at %s:%d", (int)e,
+           cudaGetErrorString(e), what, file, line);
+}
+
+void lapy_set_last_message(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+}
+
+int lapy_num_sms() {
+  static std::mutex mu;
+  static std::vector<int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+  if (cache[dev] == 0) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      sms = 1;
+    cache[dev] = sms;
+  }
+  return cache[dev];
+}
+
+static std::atomic<long long> g_launches{0};
+static std::mutex g_prof_mu;
+static bool g_prof_on = false;
+// pcg_ms, pcg_solves, pcg_iters, rows, nnz, bytes (algorithmic)
+static double g_prof[8] = {0};
+
+void lapy_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+bool lapy_profile_enabled() { return g_prof_on; }
+
+void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int eb) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  g_prof[0] += ms;
+  g_prof[1] += 1;
+  g_prof[2] += (double)iters;
+  g_prof[3] += (double)rows;
+  g_prof[4] += (double)nnz;
+  // algorithmic bytes of the fused Jacobi-PCG iteration over the rows it
+  // touched: matrix (value + column index per nonzero, row pointer per row),
+  // 11 vector streams of p values and 2 of the Jacobi diagonal
+  g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (4 + 11.0 * p * eb + 2.0 * eb);
+}
+
+extern "C" long long lapy_launch_count(void) { return g_launches.load(); }
+
+extern "C" void lapy_profile_enable(int on) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  g_prof_on = on != 0;
+}
+
+extern "C" void lapy_profile_reset(void) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  for (double& x : g_prof) x = 0;
+}
+
+extern "C" int lapy_profile_read(double* out, int n) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  for (int i = 0; i < n && i < 8; ++i) out[i] = g_prof[i];
+  return 0;
+}
+
+extern "C" int lapy_version(void) { return 10000; }
+
+extern "C" const char* lapy_status_string(int status) {
+  switch (status) {
+    case LAPY_OK: return "ok";
+    case LAPY_ERR_INVALID: return "invalid argument";
+    case LAPY_ERR_CUDA: return "CUDA error";
+    case LAPY_ERR_NOCONV: return "no convergence within the iteration cap";
+    case LAPY_ERR_BREAKDOWN: return "Krylov breakdown";
+    case LAPY_ERR_NAN: return "NaN or Inf in the iteration";
+    case LAPY_ERR_TIMEOUT: return "bounded device-side wait timed out";
+    case LAPY_ERR_WORKSPACE: return "workspace too small";
+    case LAPY_ERR_PATTERN: return "matrix pattern not contained in the stiffness pattern";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char* lapy_last_error(void) { return g_last_error; }

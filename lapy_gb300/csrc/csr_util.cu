@@ -1,0 +1,148 @@
+// CSR helpers: diagonal positions, pattern maps, mean edge length.
+#include "common.cuh"
+
+namespace lapy {
+
+__global__ void diag_index_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                                  const int32_t* __restrict__ indices, int32_t* __restrict__ pos) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int32_t lo = indptr[r], hi = indptr[r + 1] - 1, found = -1;
+  while (lo <= hi) {  // indices are sorted inside each row
+    const int32_t mid = (lo + hi) >> 1;
+    const int32_t c = indices[mid];
+    if (c == (int32_t)r) { found = mid; break; }
+    if (c < (int32_t)r) lo = mid + 1; else hi = mid - 1;
+  }
+  pos[r] = found;
+}
+
+__global__ void pattern_map_kernel(int64_t n, const int32_t* __restrict__ a_ptr,
+                                   const int32_t* __restrict__ a_idx,
+                                   const int32_t* __restrict__ b_ptr,
+                                   const int32_t* __restrict__ b_idx, int32_t* __restrict__ pos,
+                                   int* missing) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (int32_t k = b_ptr[r]; k < b_ptr[r + 1]; ++k) {
+    const int32_t c = b_idx[k];
+    int32_t lo = a_ptr[r], hi = a_ptr[r + 1] - 1, found = -1;
+    while (lo <= hi) {
+      const int32_t mid = (lo + hi) >> 1;
+      const int32_t ac = a_idx[mid];
+      if (ac == c) { found = mid; break; }
+      if (ac < c) lo = mid + 1; else hi = mid - 1;
+    }
+    pos[k] = found;
+    if (found < 0) atomicExch(missing, 1);
+  }
+}
+
+constexpr int kEdgeBlocks = 1024;
+
+// Sum of edge lengths (strict upper triangle) and edge count, per block.
+template <typename T>
+__global__ void edge_len_kernel(const T* __restrict__ v, int64_t n, const int32_t* __restrict__ indptr,
+                                const int32_t* __restrict__ indices, double* __restrict__ psum,
+                                long long* __restrict__ pcnt) {
+  __shared__ double sh[32];
+  __shared__ long long shc[32];
+  double s = 0.0;
+  long long c = 0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const T x0 = v[3 * r], y0 = v[3 * r + 1], z0 = v[3 * r + 2];
+    for (int32_t k = indptr[r]; k < indptr[r + 1]; ++k) {
+      const int32_t j = indices[k];
+      if (j <= r) continue;
+      const T dx = x0 - v[3 * (int64_t)j], dy = y0 - v[3 * (int64_t)j + 1],
+              dz = z0 - v[3 * (int64_t)j + 2];
+      // tria_mesh.py:745-747: sqrt(((v_i - v_j) ** 2).sum(1)) in the coordinate type
+      T q = dx * dx;
+      q = q + dy * dy;
+      q = q + dz * dz;
+      s += (double)sqrt(q);
+      c += 1;
+    }
+  }
+  s = block_sum(s, sh);
+  c = block_sum(c, shc);
+  if (threadIdx.x == 0) {
+    psum[blockIdx.x] = s;
+    pcnt[blockIdx.x] = c;
+  }
+}
+
+__global__ void edge_len_final_kernel(const double* psum, const long long* pcnt, int nb, double* out) {
+  __shared__ double sh[32];
+  __shared__ long long shc[32];
+  double s = 0.0;
+  long long c = 0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    s += psum[i];
+    c += pcnt[i];
+  }
+  s = block_sum(s, sh);
+  c = block_sum(c, shc);
+  if (threadIdx.x == 0) out[0] = c ? s / (double)c : 0.0;
+}
+
+}  // namespace lapy
+
+using namespace lapy;
+
+extern "C" int lapy_csr_diag_index(int64_t n, const int32_t* indptr, const int32_t* indices,
+                                   int32_t* diag_pos, void* stream) {
+  if (n <= 0 || !indptr || !indices || !diag_pos) return LAPY_ERR_INVALID;
+  diag_index_kernel<<<lapy_ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(n, indptr, indices, diag_pos);
+  return lapy_check_launch("diag_index_kernel");
+}
+
+extern "C" int lapy_csr_pattern_map(int64_t n, const int32_t* a_indptr, const int32_t* a_indices,
+                                    const int32_t* b_indptr, const int32_t* b_indices, int64_t b_nnz,
+                                    int32_t* pos, void* work, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n <= 0 || !a_indptr || !a_indices || !b_indptr || !b_indices || !pos || b_nnz < 0 || !work)
+    return LAPY_ERR_INVALID;
+  int* flag = (int*)work;
+  LAPY_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), stream));
+  pattern_map_kernel<<<lapy_ceil_div(n, 256), 256, 0, stream>>>(n, a_indptr, a_indices, b_indptr,
+                                                                b_indices, pos, flag);
+  LAPY_TRY(lapy_check_launch("pattern_map_kernel"));
+  int missing = 0;
+  LAPY_CUDA_TRY(cudaMemcpyAsync(&missing, flag, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (missing) {
+    lapy_set_last_message("csr_pattern_map: an entry of the second matrix is not in A's pattern");
+    return LAPY_ERR_PATTERN;
+  }
+  return LAPY_OK;
+}
+
+extern "C" size_t lapy_avg_edge_length_workspace_bytes(int64_t n) {
+  (void)n;
+  return kEdgeBlocks * (sizeof(double) + sizeof(long long)) + 512;
+}
+
+extern "C" int lapy_avg_edge_length(const void* v, int coords_f32, int64_t n, const int32_t* indptr,
+                                    const int32_t* indices, double* out, void* work, size_t ws_bytes,
+                                    void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (!v || n <= 0 || !indptr || !indices || !out || !work) return LAPY_ERR_INVALID;
+  if (ws_bytes < lapy_avg_edge_length_workspace_bytes(n)) return LAPY_ERR_WORKSPACE;
+  char* base = (char*)(((uintptr_t)work + 255) & ~uintptr_t(255));
+  double* psum = (double*)base;
+  long long* pcnt = (long long*)(base + kEdgeBlocks * sizeof(double));
+  double* dout = (double*)(base + kEdgeBlocks * (sizeof(double) + sizeof(long long)));
+  const unsigned nb = (unsigned)std::min<int64_t>(kEdgeBlocks, std::max<int64_t>(1, lapy_ceil_div(n, 256)));
+  if (coords_f32)
+    edge_len_kernel<float><<<nb, 256, 0, stream>>>((const float*)v, n, indptr, indices, psum, pcnt);
+  else
+    edge_len_kernel<double><<<nb, 256, 0, stream>>>((const double*)v, n, indptr, indices, psum, pcnt);
+  LAPY_TRY(lapy_check_launch("edge_len_kernel"));
+  edge_len_final_kernel<<<1, 256, 0, stream>>>(psum, pcnt, (int)nb, dout);
+  LAPY_TRY(lapy_check_launch("edge_len_final_kernel"));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(out, dout, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+  return LAPY_OK;
+}

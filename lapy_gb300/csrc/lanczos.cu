@@ -1,0 +1,710 @@
+// Block shift-invert Lanczos for A x = lambda M x on a batch of meshes.
+//
+// The operator OP = (A - sigma M)^-1 M is self-adjoint in the M inner product.
+// Each block step applies OP to the newest basis block (inner solves: FP32
+// PCG inside FP64 iterative refinement), orthogonalises the result against
+// the whole basis twice (classical Gram-Schmidt, FP64), stores the projection
+// coefficients as a block column of T = Q' M OP M Q, and M-orthonormalises
+// the block with two Cholesky-QR passes.  No restarts: the basis is kept
+// (HBM holds it easily), so the projected matrix is the Rayleigh quotient of
+// OP on the whole Krylov space.  At check points the top eigenpairs of T
+// (FP64, dense.cu) give residual estimates ||B_m S_last,i|| / |theta_i|.  A
+// converged segment is frozen; when all are, the Ritz vectors X = Q S enter a
+// final FP64 Rayleigh-Ritz step with the exact A and M, which returns the
+// eigenvalues (ascending) and M-orthonormal eigenvectors.
+//
+// This is the method of lapy/solver.py:667-716 (eigsh in shift-invert mode
+// with OPinv = splu(A - sigma M).solve): same operator, same sigma, same
+// output convention; ARPACK's implicit restarts are replaced by a full basis
+// and the sparse LU by iterative inner solves.
+#include <cmath>
+#include <vector>
+#include "blas.cuh"
+#include "dense.cuh"
+#include "solve.cuh"
+#include "spmv.cuh"
+
+namespace lapy {
+
+static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+__global__ void rand_fill_kernel(int64_t n, uint64_t seed, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t h = (uint64_t)i * 0x9E3779B97F4A7C15ull + seed * 0xD1B54A32D192ED03ull + 0x632BE59BD9B4E019ull;
+  h ^= h >> 31; h *= 0xBF58476D1CE4E5B9ull; h ^= h >> 27; h *= 0x94D049BB133111EBull; h ^= h >> 31;
+  out[i] = ((double)(h >> 11) * (1.0 / 9007199254740992.0)) - 0.5;
+}
+
+// Zero rows of segments that are not active (block per chunk).
+__global__ void zero_inactive_kernel(double* __restrict__ X, int ncol, const int32_t* __restrict__ chunk_row,
+                                     const int32_t* __restrict__ chunk_seg, const int32_t* __restrict__ active) {
+  const int c = blockIdx.x;
+  if (active[chunk_seg[c]]) return;
+  const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
+  for (int64_t i = r0 * ncol + threadIdx.x; i < r1 * ncol; i += blockDim.x) X[i] = 0.0;
+}
+
+// Block-strided addressing: element (row, a) of a matrix stored as blocks of
+// `bs` columns, block stride `bst` elements: base[(a/bs)*bst + row*bs + a%bs].
+struct BMat {
+  const double* base;
+  int bs;
+  int64_t bst;
+  __device__ __forceinline__ double at(int64_t row, int a) const {
+    return base[(int64_t)(a / bs) * bst + row * bs + (a % bs)];
+  }
+};
+
+constexpr int kTile = 16;
+
+// partial[c][a][b] = sum over the chunk's rows of X(row, a) * Y(row, b)
+__global__ void __launch_bounds__(256) gemm_tn_partial_kernel(BMat X, int na, BMat Y, int nb,
+                                                              const int32_t* __restrict__ chunk_row,
+                                                              const int32_t* __restrict__ chunk_seg,
+                                                              const int32_t* __restrict__ active,
+                                                              double* __restrict__ partial) {
+  const int c = blockIdx.x;
+  const int a = blockIdx.y * kTile + threadIdx.x / kTile;
+  const int b = blockIdx.z * kTile + threadIdx.x % kTile;
+  const bool act = !active || active[chunk_seg[c]];
+  double acc = 0.0;
+  if (act && a < na && b < nb) {
+    const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
+    for (int64_t r = r0; r < r1; ++r) acc += X.at(r, a) * Y.at(r, b);
+  }
+  if (a < na && b < nb) partial[((int64_t)c * na + a) * nb + b] = acc;
+}
+
+// out[s][a][b] (leading dim ldo) = sum over chunks of segment s
+__global__ void gemm_tn_reduce_kernel(const double* __restrict__ partial, int na, int nb,
+                                      const int32_t* __restrict__ seg_chunk, double* __restrict__ out,
+                                      int64_t out_seg_stride, int ldo) {
+  const int s = blockIdx.x;
+  const int c0 = seg_chunk[s], c1 = seg_chunk[s + 1];
+  for (int e = blockIdx.y * blockDim.x + threadIdx.x; e < na * nb; e += gridDim.y * blockDim.x) {
+    const int a = e / nb, b = e % nb;
+    double acc = 0.0;
+    for (int c = c0; c < c1; ++c) acc += partial[((int64_t)c * na + a) * nb + b];
+    out[(int64_t)s * out_seg_stride + (int64_t)a * ldo + b] = acc;
+  }
+}
+
+// Y(row, b) = beta*Y(row, b) + alpha * sum_a X(row, a) * H_s[a*ldh + b]
+__global__ void __launch_bounds__(256) gemm_nn_kernel(BMat X, int na, const double* __restrict__ H,
+                                                      int64_t h_seg_stride, int ldh, double* __restrict__ Y,
+                                                      int ldy, int nb, double alpha, double beta,
+                                                      const int32_t* __restrict__ chunk_row,
+                                                      const int32_t* __restrict__ chunk_seg,
+                                                      const int32_t* __restrict__ active) {
+  const int c = blockIdx.x;
+  const int s = chunk_seg[c];
+  if (active && !active[s]) return;
+  const double* Hs = H + (int64_t)s * h_seg_stride;
+  const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
+  for (int64_t e = r0 * nb + threadIdx.x; e < r1 * nb; e += blockDim.x) {
+    const int64_t row = e / nb;
+    const int b = (int)(e - row * nb);
+    double acc = 0.0;
+    for (int a = 0; a < na; ++a) acc += X.at(row, a) * Hs[(int64_t)a * ldh + b];
+    const int64_t o = row * ldy + b;
+    Y[o] = (beta == 0.0) ? alpha * acc : beta * Y[o] + alpha * acc;
+  }
+}
+
+// Cholesky of the p x p Gram matrix of every segment: G = R' R (R upper).
+// Inactive segments get R = I.  fail[s] = 1 when G is not numerically SPD.
+__global__ void chol_small_kernel(int nseg, int p, const double* __restrict__ G, double* __restrict__ R,
+                                  const int32_t* __restrict__ active, int32_t* __restrict__ fail) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const double* g = G + (int64_t)s * p * p;
+  double* r = R + (int64_t)s * p * p;
+  for (int i = 0; i < p * p; ++i) r[i] = 0.0;
+  if (!active[s]) {
+    for (int i = 0; i < p; ++i) r[i * p + i] = 1.0;
+    return;
+  }
+  double gmax = 0.0;
+  for (int i = 0; i < p; ++i) gmax = fmax(gmax, fabs(g[i * p + i]));
+  int bad = 0;
+  for (int j = 0; j < p; ++j) {
+    double dsum = 0.5 * (g[j * p + j] + g[j * p + j]);
+    for (int k = 0; k < j; ++k) dsum -= r[k * p + j] * r[k * p + j];
+    if (!(dsum > 1e-28 * gmax) || !isfinite(dsum)) { bad = 1; dsum = fmax(gmax, 1e-300) * 1e-28; }
+    const double rjj = sqrt(dsum);
+    r[j * p + j] = rjj;
+    for (int i = j + 1; i < p; ++i) {
+      double v = 0.5 * (g[j * p + i] + g[i * p + j]);
+      for (int k = 0; k < j; ++k) v -= r[k * p + j] * r[k * p + i];
+      r[j * p + i] = v / rjj;
+    }
+  }
+  fail[s] = bad;
+}
+
+// W(row, :) = W(row, :) * R_s^-1  (R upper triangular, p x p)
+__global__ void trsm_right_kernel(double* __restrict__ W, int p, const double* __restrict__ R,
+                                  const int32_t* __restrict__ chunk_row, const int32_t* __restrict__ chunk_seg,
+                                  int nchunk) {
+  const int c = blockIdx.x;
+  const int s = chunk_seg[c];
+  const double* r = R + (int64_t)s * p * p;
+  const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
+  for (int64_t row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
+    double x[16];
+    double* w = W + row * p;
+    for (int j = 0; j < p; ++j) {
+      double v = w[j];
+      for (int i = 0; i < j; ++i) v -= x[i] * r[i * p + j];
+      x[j] = v / r[j * p + j];
+    }
+    for (int j = 0; j < p; ++j) w[j] = x[j];
+  }
+}
+
+// C_s = A_s * B_s for p x p (used for B_j = R2 R1)
+__global__ void small_matmul_kernel(int nseg, int p, const double* __restrict__ A, const double* __restrict__ B,
+                                    double* __restrict__ C) {
+  const int s = blockIdx.x;
+  const double* a = A + (int64_t)s * p * p;
+  const double* b = B + (int64_t)s * p * p;
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
+    const int i = e / p, j = e % p;
+    double acc = 0.0;
+    for (int k = 0; k < p; ++k) acc += a[i * p + k] * b[k * p + j];
+    C[(int64_t)s * p * p + e] = acc;
+  }
+}
+
+// T_s[r][jp + c] = T_s[jp + c][r] = H_s[r][c] for r < (j+1)p (diagonal block symmetrised)
+__global__ void store_T_kernel(int p, int j, const double* __restrict__ H, int64_t h_seg_stride,
+                               double* __restrict__ T, int lda, const int32_t* __restrict__ active) {
+  const int s = blockIdx.x;
+  if (!active[s]) return;
+  const double* h = H + (int64_t)s * h_seg_stride;
+  double* t = T + (int64_t)s * lda * lda;
+  const int rows = (j + 1) * p;
+  for (int e = threadIdx.x; e < rows * p; e += blockDim.x) {
+    const int r = e / p, c = e % p;
+    double v = h[(int64_t)r * p + c];
+    if (r >= j * p) {
+      const int a = r - j * p;
+      v = 0.5 * (v + h[(int64_t)(j * p + c) * p + a]);
+    }
+    t[(int64_t)r * lda + j * p + c] = v;
+    t[(int64_t)(j * p + c) * lda + r] = v;
+  }
+}
+
+__global__ void copy_T_kernel(const double* __restrict__ T, double* __restrict__ Tc, int lda, int m,
+                              const int32_t* __restrict__ active) {
+  const int s = blockIdx.x;
+  if (!active[s]) return;
+  const double* t = T + (int64_t)s * lda * lda;
+  double* tc = Tc + (int64_t)s * lda * lda;
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+    const int r = e / m, c = e % m;
+    tc[(int64_t)r * lda + c] = t[(int64_t)r * lda + c];
+  }
+}
+
+// Residual estimates of the k wanted Ritz pairs; freeze converged segments.
+__global__ void conv_check_kernel(int nseg, int p, int m, int lda, int keff, int k, double tol,
+                                  const double* __restrict__ theta, const double* __restrict__ S,
+                                  const double* __restrict__ Bm, const int32_t* __restrict__ fail,
+                                  int32_t* __restrict__ nconv, int32_t* __restrict__ active,
+                                  double* __restrict__ Sfinal, double* __restrict__ theta_final,
+                                  double* __restrict__ resid_out) {
+  __shared__ double sh[32];
+  __shared__ int s_ok;
+  const int s = blockIdx.x;
+  if (!active[s]) return;
+  const double* th = theta + (int64_t)s * keff;
+  const double* Ss = S + (int64_t)s * lda * keff;
+  const double* B = Bm + (int64_t)s * p * p;
+  // a rank-deficient new block means the Krylov space became invariant: the
+  // Ritz pairs are then exact and are accepted
+  const double tol_s = fail[s] ? 1e300 : tol;
+  double worst = 0.0;
+  int cnt = 0;
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    double r2 = 0.0;
+    for (int a = 0; a < p; ++a) {
+      double v = 0.0;
+      for (int b = 0; b < p; ++b) v += B[a * p + b] * Ss[(int64_t)(m - p + b) * keff + i];
+      r2 += v * v;
+    }
+    const double res = sqrt(r2) / fmax(fabs(th[i]), 1e-300);
+    worst = fmax(worst, isfinite(res) ? res : 1e300);
+    cnt += (res <= tol_s) ? 1 : 0;
+  }
+  cnt = block_sum(cnt, (int*)sh);
+  // block max
+  for (int o = 16; o > 0; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = worst;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double w = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) w = fmax(w, sh[i]);
+    resid_out[s] = w;
+    nconv[s] = cnt;
+    s_ok = (w <= tol_s);
+  }
+  __syncthreads();
+  if (!s_ok) return;
+  for (int64_t e = threadIdx.x; e < (int64_t)lda * keff; e += blockDim.x)
+    Sfinal[(int64_t)s * lda * keff + e] = Ss[e];
+  for (int i = threadIdx.x; i < keff; i += blockDim.x) theta_final[(int64_t)s * keff + i] = th[i];
+  __syncthreads();
+  if (threadIdx.x == 0) active[s] = 0;
+}
+
+// Final Rayleigh-Ritz, dense part (one CTA per segment):
+//   Mk = L L', C = L^-1 Ak L^-T, stored negated (so the top eigenpairs of -C
+//   are the smallest of C).
+__global__ void rr_prepare_kernel(int keff, double* __restrict__ Ak, double* __restrict__ Mk,
+                                  double* __restrict__ Cneg, int32_t* __restrict__ fail) {
+  const int s = blockIdx.x;
+  double* A = Ak + (int64_t)s * keff * keff;
+  double* L = Mk + (int64_t)s * keff * keff;
+  double* C = Cneg + (int64_t)s * keff * keff;
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  // symmetrise both
+  for (int e = threadIdx.x; e < keff * keff; e += blockDim.x) {
+    const int i = e / keff, j = e % keff;
+    if (i < j) {
+      const double a = 0.5 * (A[i * keff + j] + A[j * keff + i]);
+      A[i * keff + j] = a; A[j * keff + i] = a;
+      const double m = 0.5 * (L[i * keff + j] + L[j * keff + i]);
+      L[i * keff + j] = m; L[j * keff + i] = m;
+    }
+  }
+  __syncthreads();
+  // Cholesky (lower, left-looking), L overwrites Mk's lower triangle
+  for (int j = 0; j < keff; ++j) {
+    if (threadIdx.x == 0) {
+      double d = L[j * keff + j];
+      for (int k = 0; k < j; ++k) d -= L[j * keff + k] * L[j * keff + k];
+      if (!(d > 0) || !isfinite(d)) { bad = 1; d = 1e-300; }
+      L[j * keff + j] = sqrt(d);
+    }
+    __syncthreads();
+    const double ljj = L[j * keff + j];
+    for (int i = j + 1 + threadIdx.x; i < keff; i += blockDim.x) {
+      double v = L[i * keff + j];
+      for (int k = 0; k < j; ++k) v -= L[i * keff + k] * L[j * keff + k];
+      L[i * keff + j] = v / ljj;
+    }
+    __syncthreads();
+  }
+  // Z = L^-1 A  (column per thread), stored in C
+  for (int col = threadIdx.x; col < keff; col += blockDim.x) {
+    for (int i = 0; i < keff; ++i) {
+      double v = A[i * keff + col];
+      for (int k = 0; k < i; ++k) v -= L[i * keff + k] * C[k * keff + col];
+      C[i * keff + col] = v / L[i * keff + i];
+    }
+  }
+  __syncthreads();
+  // C = L^-1 Z'  : transpose Z into A (scratch), then forward-substitute
+  for (int e = threadIdx.x; e < keff * keff; e += blockDim.x) {
+    const int i = e / keff, j = e % keff;
+    A[j * keff + i] = C[i * keff + j];
+  }
+  __syncthreads();
+  for (int col = threadIdx.x; col < keff; col += blockDim.x) {
+    for (int i = 0; i < keff; ++i) {
+      double v = A[i * keff + col];
+      for (int k = 0; k < i; ++k) v -= L[i * keff + k] * C[k * keff + col];
+      C[i * keff + col] = v / L[i * keff + i];
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < keff * keff; e += blockDim.x) C[e] = -C[e];
+  if (threadIdx.x == 0) fail[s] = bad;
+}
+
+// Yv = L^-T V  (V: keff x k eigenvectors of -C), written over V; lambda = -theta.
+__global__ void rr_finish_kernel(int keff, int k, const double* __restrict__ Lm, double* __restrict__ V,
+                                 const double* __restrict__ theta, double* __restrict__ evals) {
+  const int s = blockIdx.x;
+  const double* L = Lm + (int64_t)s * keff * keff;
+  double* v = V + (int64_t)s * keff * k;
+  for (int col = threadIdx.x; col < k; col += blockDim.x) {
+    for (int i = keff - 1; i >= 0; --i) {
+      double x = v[(int64_t)i * k + col];
+      for (int j = i + 1; j < keff; ++j) x -= L[j * keff + i] * v[(int64_t)j * k + col];
+      v[(int64_t)i * k + col] = x / L[i * keff + i];
+    }
+    evals[(int64_t)s * k + col] = -theta[(int64_t)s * k + col];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+struct EigPlan {
+  int64_t n, nnz;
+  int nseg, p, k, keff, mb, lda;
+  ChunkTable ct;   // PCG chunks
+  ChunkTable gt;   // GEMM chunks (larger)
+};
+
+struct EigPtrs {
+  void* ct_mem; void* gt_mem;
+  int32_t* diag_pos; double* k64; float* k32; double* dinv64; float* dinv32;
+  double* basis; double* Y; double* W; double* MW;
+  void* ir_ws; size_t ir_bytes;
+  double* partial;
+  double* H; double* Hsum; double* G; double* R1; double* R2; double* Bm;
+  double* T; double* Tc; double* theta; double* S; double* eigw;
+  double* Sfinal; double* theta_final;
+  double* X; double* AX; double* MX;
+  double* Ak; double* Mk; double* Cneg; double* theta2; double* V; double* eigw2;
+  int32_t* active; int32_t* nsize; int32_t* fail; int32_t* nconv; double* resid;
+};
+
+static void plan_eig(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, int k, int p, int max_vectors,
+                     EigPlan* P) {
+  P->n = n; P->nnz = nnz; P->nseg = nseg; P->p = p; P->k = k;
+  P->keff = k + p;
+  P->mb = std::max((max_vectors + p - 1) / p, (P->keff + 2 * p + p - 1) / p + 1);
+  P->lda = P->mb * p;
+  std::vector<int32_t> srow(seg_row, seg_row + nseg + 1);
+  plan_chunks(srow.data(), nseg, 4 * lapy_num_sms(), &P->ct);
+  plan_chunks(srow.data(), nseg, 2 * lapy_num_sms(), &P->gt);
+}
+
+static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* r = base ? base + off : nullptr;
+    off += a256(bytes);
+    return r;
+  };
+  const int64_t n = P.n, nnz = P.nnz;
+  const int ns = P.nseg, p = P.p, keff = P.keff, lda = P.lda, k = P.k;
+  EigPtrs e;
+  e.ct_mem = take(chunk_table_bytes(ns, P.ct.nchunk));
+  e.gt_mem = take(chunk_table_bytes(ns, P.gt.nchunk));
+  e.diag_pos = (int32_t*)take(4 * n);
+  e.k64 = (double*)take(8 * nnz);
+  e.k32 = (float*)take(4 * nnz);
+  e.dinv64 = (double*)take(8 * n);
+  e.dinv32 = (float*)take(4 * n);
+  e.basis = (double*)take(8 * (size_t)(P.mb + 1) * n * p);
+  e.Y = (double*)take(8 * n * p);
+  e.W = (double*)take(8 * n * p);
+  e.MW = (double*)take(8 * n * p);
+  e.ir_bytes = ir_workspace_bytes(n, p, ns, P.ct.nchunk, 1, kPrecJacobi);
+  e.ir_ws = take(e.ir_bytes);
+  const size_t part_elems = (size_t)P.gt.nchunk * std::max((size_t)lda * p, (size_t)keff * keff);
+  e.partial = (double*)take(8 * part_elems);
+  e.H = (double*)take(8 * (size_t)ns * lda * p);
+  e.Hsum = (double*)take(8 * (size_t)ns * lda * p);
+  e.G = (double*)take(8 * (size_t)ns * p * p);
+  e.R1 = (double*)take(8 * (size_t)ns * p * p);
+  e.R2 = (double*)take(8 * (size_t)ns * p * p);
+  e.Bm = (double*)take(8 * (size_t)ns * p * p);
+  e.T = (double*)take(8 * (size_t)ns * lda * lda);
+  e.Tc = (double*)take(8 * (size_t)ns * lda * lda);
+  e.theta = (double*)take(8 * (size_t)ns * keff);
+  e.S = (double*)take(8 * (size_t)ns * lda * keff);
+  e.eigw = (double*)take(8 * (size_t)ns * sym_eig_work_doubles(lda, keff));
+  e.Sfinal = (double*)take(8 * (size_t)ns * lda * keff);
+  e.theta_final = (double*)take(8 * (size_t)ns * keff);
+  e.X = (double*)take(8 * n * keff);
+  e.AX = (double*)take(8 * n * keff);
+  e.MX = (double*)take(8 * n * keff);
+  e.Ak = (double*)take(8 * (size_t)ns * keff * keff);
+  e.Mk = (double*)take(8 * (size_t)ns * keff * keff);
+  e.Cneg = (double*)take(8 * (size_t)ns * keff * keff);
+  e.theta2 = (double*)take(8 * (size_t)ns * k);
+  e.V = (double*)take(8 * (size_t)ns * keff * k);
+  e.eigw2 = (double*)take(8 * (size_t)ns * sym_eig_work_doubles(keff, k));
+  e.active = (int32_t*)take(4 * ns);
+  e.nsize = (int32_t*)take(4 * ns);
+  e.fail = (int32_t*)take(4 * ns);
+  e.nconv = (int32_t*)take(4 * ns);
+  e.resid = (double*)take(8 * ns);
+  if (q) *q = e;
+  return off + 256;
+}
+
+struct EigOps {
+  const EigPlan& P;
+  const EigPtrs& e;
+  const int32_t* indptr;
+  const int32_t* indices;
+  const double* a_vals;
+  const double* m_vals;
+  int m_is_diag;
+  int G;
+  cudaStream_t st;
+
+  int apply_M(const double* X, double* Y, int ncol) const {
+    if (m_is_diag) {
+      return lapy_diag_mm_f64(P.n, m_vals, ncol, X, Y, 1.0, 0.0, st);
+    }
+    return csr_spmm<double>(P.n, indptr, indices, m_vals, ncol, X, Y, 1.0, 0.0, G, st);
+  }
+  // out_s (na x nb, ldo) = X' Y per segment
+  int gemm_tn(BMat X, int na, BMat Y, int nb, double* out, int64_t out_stride, int ldo, const int32_t* act) const {
+    dim3 grid(P.gt.nchunk, lapy_ceil_div(na, kTile), lapy_ceil_div(nb, kTile));
+    gemm_tn_partial_kernel<<<grid, 256, 0, st>>>(X, na, Y, nb, P.gt.chunk_row, P.gt.chunk_seg, act, e.partial);
+    LAPY_TRY(lapy_check_launch("gemm_tn_partial_kernel"));
+    dim3 g2(P.nseg, std::max(1u, std::min(64u, lapy_ceil_div((int64_t)na * nb, 256))));
+    gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, na, nb, P.gt.seg_chunk, out, out_stride, ldo);
+    return lapy_check_launch("gemm_tn_reduce_kernel");
+  }
+  int gemm_nn(BMat X, int na, const double* H, int64_t hs, int ldh, double* Y, int ldy, int nb, double alpha,
+              double beta, const int32_t* act) const {
+    gemm_nn_kernel<<<P.gt.nchunk, 256, 0, st>>>(X, na, H, hs, ldh, Y, ldy, nb, alpha, beta, P.gt.chunk_row,
+                                               P.gt.chunk_seg, act);
+    return lapy_check_launch("gemm_nn_kernel");
+  }
+  // M-orthonormalise W (n x p) in place with two Cholesky-QR passes; Bm = R2 R1.
+  int chol_qr2(double* W) const {
+    const int p = P.p;
+    BMat Wm{W, p, 0};
+    for (int pass = 0; pass < 2; ++pass) {
+      LAPY_TRY(apply_M(W, e.MW, p));
+      BMat MWm{e.MW, p, 0};
+      LAPY_TRY(gemm_tn(Wm, p, MWm, p, e.G, (int64_t)p * p, p, e.active));
+      double* R = pass == 0 ? e.R1 : e.R2;
+      chol_small_kernel<<<lapy_ceil_div(P.nseg, 64), 64, 0, st>>>(P.nseg, p, e.G, R, e.active, e.fail);
+      LAPY_TRY(lapy_check_launch("chol_small_kernel"));
+      trsm_right_kernel<<<P.gt.nchunk, 128, 0, st>>>(W, p, R, P.gt.chunk_row, P.gt.chunk_seg, P.gt.nchunk);
+      LAPY_TRY(lapy_check_launch("trsm_right_kernel"));
+    }
+    small_matmul_kernel<<<P.nseg, 64, 0, st>>>(P.nseg, p, e.R2, e.R1, e.Bm);
+    return lapy_check_launch("small_matmul_kernel");
+  }
+};
+
+struct EigResult {
+  std::vector<int32_t> status;
+  std::vector<int32_t> nbasis;
+  int64_t inner_iters = 0;
+  int blocks = 0;
+};
+
+static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, const int32_t* indices,
+                    const double* a_vals, const double* m_vals, int m_is_diag, double sigma, double tol,
+                    double inner_rtol, double round_rtol, int inner_maxiter, uint64_t seed, double* evals,
+                    double* evecs, cudaStream_t st, EigResult* res) {
+  const int64_t n = P.n;
+  const int p = P.p, ns = P.nseg, keff = P.keff, lda = P.lda, k = P.k;
+  const int G = spmm_pick_group(n, P.nnz);
+  EigOps ops{P, e, indptr, indices, a_vals, m_vals, m_is_diag, G, st};
+  ChunkTable ct = P.ct, gt = P.gt;
+  LAPY_TRY(upload_chunk_table(&ct, e.ct_mem, st));
+  LAPY_TRY(upload_chunk_table(&gt, e.gt_mem, st));
+  const_cast<EigPlan&>(P).ct = ct;
+  const_cast<EigPlan&>(P).gt = gt;
+
+  // K = A - sigma M (f64 and f32), Jacobi diagonal
+  LAPY_TRY(lapy_csr_diag_index(n, indptr, indices, e.diag_pos, st));
+  if (m_is_diag) {
+    LAPY_CUDA_TRY(cudaMemcpyAsync(e.k64, a_vals, 8 * P.nnz, cudaMemcpyDeviceToDevice, st));
+    LAPY_TRY(add_diag(n, e.diag_pos, -sigma, m_vals, e.k64, st));
+  } else {
+    LAPY_TRY(vec_axpby(P.nnz, 1.0, a_vals, -sigma, m_vals, e.k64, st));
+  }
+  LAPY_TRY(cast_f64_f32(P.nnz, e.k64, e.k32, st));
+  LAPY_TRY(jacobi_inverse(n, e.diag_pos, e.k64, e.dinv64, e.dinv32, st));
+  SysMatrix K;
+  K.n = n; K.nnz = P.nnz; K.indptr = indptr; K.indices = indices;
+  K.k64 = e.k64; K.k32 = e.k32; K.dinv64 = e.dinv64; K.dinv32 = e.dinv32;
+
+  std::vector<int32_t> hact(ns, 1), hnsize(ns, 0);
+  LAPY_CUDA_TRY(cudaMemcpyAsync(e.active, hact.data(), 4 * ns, cudaMemcpyHostToDevice, st));
+  LAPY_CUDA_TRY(cudaMemsetAsync(e.T, 0, 8 * (size_t)ns * lda * lda, st));
+  LAPY_CUDA_TRY(cudaMemsetAsync(e.Sfinal, 0, 8 * (size_t)ns * lda * keff, st));
+  LAPY_CUDA_TRY(cudaMemsetAsync(e.fail, 0, 4 * ns, st));
+
+  // Q_0: random, M-orthonormal
+  double* Q0 = e.basis;
+  rand_fill_kernel<<<lapy_ceil_div(n * p, 256), 256, 0, st>>>(n * p, seed, Q0);
+  LAPY_TRY(lapy_check_launch("rand_fill_kernel"));
+  LAPY_TRY(ops.chol_qr2(Q0));
+
+  std::vector<int32_t> hfail(ns);
+  res->status.assign(ns, LAPY_ERR_NOCONV);
+  res->nbasis.assign(ns, 0);
+  // First check once the basis holds ~2.5 k vectors (shift-invert Lanczos
+  // needs 3-5 k); afterwards the gap to k converged pairs sets the stride.
+  const int first_check = std::max((keff + p + p - 1) / p, (int)std::ceil(2.5 * k / p));
+  int next_check = first_check;
+  std::vector<int32_t> hnconv(ns);
+  int j = 0;
+  bool all_done = false;
+  std::vector<int32_t> seg_conv_blocks(ns, 0);
+  for (j = 0; j < P.mb && !all_done; ++j) {
+    double* Qj = e.basis + (size_t)j * n * p;
+    double* Qn = e.basis + (size_t)(j + 1) * n * p;
+    // Y = M Q_j ; W = K^-1 Y
+    LAPY_TRY(ops.apply_M(Qj, e.Y, p));
+    zero_inactive_kernel<<<P.ct.nchunk, 256, 0, st>>>(e.Y, p, P.ct.chunk_row, P.ct.chunk_seg, e.active);
+    LAPY_TRY(lapy_check_launch("zero_inactive_kernel"));
+    IrStats irs;
+    LAPY_TRY(ir_solve(K, P.ct, p, e.Y, e.W, inner_rtol, inner_maxiter, 1, round_rtol, 16, e.ir_ws, e.ir_bytes,
+                      st, &irs, nullptr, nullptr));
+    res->inner_iters += irs.pcg_iters;
+    if (irs.status == LAPY_ERR_NAN || irs.status == LAPY_ERR_BREAKDOWN) {
+      lapy_set_last_message("eigs: inner solve failed (%s)", lapy_status_string(irs.status));
+      return irs.status;
+    }
+    // CGS2 against the basis blocks 0..j
+    const int nbasis = (j + 1) * p;
+    BMat Qm{e.basis, p, n * p};
+    BMat Wm{e.W, p, 0};
+    for (int pass = 0; pass < 2; ++pass) {
+      LAPY_TRY(ops.apply_M(e.W, e.MW, p));
+      BMat MWm{e.MW, p, 0};
+      double* Hdst = pass == 0 ? e.Hsum : e.H;
+      LAPY_TRY(ops.gemm_tn(Qm, nbasis, MWm, p, Hdst, (int64_t)lda * p, p, e.active));
+      LAPY_TRY(ops.gemm_nn(Qm, nbasis, Hdst, (int64_t)lda * p, p, e.W, p, p, -1.0, 1.0, e.active));
+      (void)Wm;
+    }
+    // Hsum += H
+    LAPY_TRY(vec_axpby((int64_t)ns * lda * p, 1.0, e.Hsum, 1.0, e.H, e.Hsum, st));
+    store_T_kernel<<<ns, 256, 0, st>>>(p, j, e.Hsum, (int64_t)lda * p, e.T, lda, e.active);
+    LAPY_TRY(lapy_check_launch("store_T_kernel"));
+    // new block
+    LAPY_CUDA_TRY(cudaMemcpyAsync(Qn, e.W, 8 * n * p, cudaMemcpyDeviceToDevice, st));
+    LAPY_TRY(ops.chol_qr2(Qn));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(hfail.data(), e.fail, 4 * ns, cudaMemcpyDeviceToHost, st));
+    const int m = (j + 1) * p;
+    const bool check = (j + 1 >= next_check) || j + 1 == P.mb;
+    LAPY_CUDA_TRY(cudaStreamSynchronize(st));
+    bool any_fail = false;
+    for (int s = 0; s < ns; ++s) any_fail |= (hact[s] && hfail[s]);
+    if (check || any_fail) {
+      for (int s = 0; s < ns; ++s) hnsize[s] = m;
+      LAPY_CUDA_TRY(cudaMemcpyAsync(e.nsize, hnsize.data(), 4 * ns, cudaMemcpyHostToDevice, st));
+      copy_T_kernel<<<ns, 256, 0, st>>>(e.T, e.Tc, lda, m, e.active);
+      LAPY_TRY(lapy_check_launch("copy_T_kernel"));
+      LAPY_TRY(sym_eig_top(ns, e.Tc, lda, e.nsize, keff, e.theta, e.S, e.eigw, e.active, st));
+      conv_check_kernel<<<ns, 128, 0, st>>>(ns, p, m, lda, keff, k, tol, e.theta, e.S, e.Bm, e.fail, e.nconv,
+                                            e.active, e.Sfinal, e.theta_final, e.resid);
+      LAPY_TRY(lapy_check_launch("conv_check_kernel"));
+      std::vector<int32_t> hact2(ns);
+      LAPY_CUDA_TRY(cudaMemcpyAsync(hact2.data(), e.active, 4 * ns, cudaMemcpyDeviceToHost, st));
+      LAPY_CUDA_TRY(cudaMemcpyAsync(hnconv.data(), e.nconv, 4 * ns, cudaMemcpyDeviceToHost, st));
+      LAPY_CUDA_TRY(cudaStreamSynchronize(st));
+      all_done = true;
+      int missing = 0;
+      for (int s = 0; s < ns; ++s) {
+        if (hact[s] && !hact2[s]) { res->status[s] = LAPY_OK; res->nbasis[s] = m; }
+        if (hact2[s]) missing = std::max(missing, k - hnconv[s]);
+        hact[s] = hact2[s];
+        all_done &= !hact[s];
+      }
+      next_check = j + 1 + std::max(1, (int)std::ceil(0.5 * missing / p));
+    }
+  }
+  res->blocks = j;
+  // segments that never converged: use their last Ritz vectors anyway (status NOCONV)
+  {
+    std::vector<int32_t> ones(ns, 1);
+    bool any = false;
+    for (int s = 0; s < ns; ++s) any |= (hact[s] != 0);
+    if (any) {
+      // copy current S/theta into the final store for still-active segments
+      for (int s = 0; s < ns; ++s) {
+        if (!hact[s]) continue;
+        LAPY_CUDA_TRY(cudaMemcpyAsync(e.Sfinal + (size_t)s * lda * keff, e.S + (size_t)s * lda * keff,
+                                      8 * (size_t)lda * keff, cudaMemcpyDeviceToDevice, st));
+        res->nbasis[s] = j * p;
+      }
+    }
+    LAPY_CUDA_TRY(cudaMemcpyAsync(e.active, ones.data(), 4 * ns, cudaMemcpyHostToDevice, st));
+    LAPY_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  // X = Q S_final (n x keff): basis blocks 0..j-1 (S rows beyond a segment's m are zero)
+  const int nb_used = j * p;
+  BMat Qm{e.basis, p, n * p};
+  LAPY_TRY(ops.gemm_nn(Qm, nb_used, e.Sfinal, (int64_t)lda * keff, keff, e.X, keff, keff, 1.0, 0.0, nullptr));
+  // final Rayleigh-Ritz with the exact A and M
+  LAPY_TRY(csr_spmm<double>(n, indptr, indices, a_vals, keff, e.X, e.AX, 1.0, 0.0, G, st));
+  LAPY_TRY(ops.apply_M(e.X, e.MX, keff));
+  BMat Xm{e.X, keff, 0}, AXm{e.AX, keff, 0}, MXm{e.MX, keff, 0};
+  LAPY_TRY(ops.gemm_tn(Xm, keff, AXm, keff, e.Ak, (int64_t)keff * keff, keff, nullptr));
+  LAPY_TRY(ops.gemm_tn(Xm, keff, MXm, keff, e.Mk, (int64_t)keff * keff, keff, nullptr));
+  rr_prepare_kernel<<<ns, 128, 0, st>>>(keff, e.Ak, e.Mk, e.Cneg, e.fail);
+  LAPY_TRY(lapy_check_launch("rr_prepare_kernel"));
+  std::vector<int32_t> hk(ns, keff);
+  LAPY_CUDA_TRY(cudaMemcpyAsync(e.nsize, hk.data(), 4 * ns, cudaMemcpyHostToDevice, st));
+  LAPY_TRY(sym_eig_top(ns, e.Cneg, keff, e.nsize, k, e.theta2, e.V, e.eigw2, nullptr, st));
+  rr_finish_kernel<<<ns, 128, 0, st>>>(keff, k, e.Mk, e.V, e.theta2, evals);
+  LAPY_TRY(lapy_check_launch("rr_finish_kernel"));
+  BMat X2{e.X, keff, 0};
+  LAPY_TRY(ops.gemm_nn(X2, keff, e.V, (int64_t)keff * k, k, evecs, k, k, 1.0, 0.0, nullptr));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(hfail.data(), e.fail, 4 * ns, cudaMemcpyDeviceToHost, st));
+  LAPY_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int s = 0; s < ns; ++s)
+    if (hfail[s] && res->status[s] == LAPY_OK) res->status[s] = LAPY_ERR_BREAKDOWN;
+  return LAPY_OK;
+}
+
+}  // namespace lapy
+
+using namespace lapy;
+
+static int eig_block_ok(int p) { return p == 1 || p == 2 || p == 4 || p == 8 || p == 16; }
+
+extern "C" size_t lapy_eigs_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, int k,
+                                            int block, int max_vectors) {
+  if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || k <= 0 || !eig_block_ok(block)) return 0;
+  EigPlan P;
+  plan_eig(n, nnz, nseg, seg_row, k, block, max_vectors, &P);
+  return layout_eig(P, nullptr, nullptr);
+}
+
+extern "C" int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const int32_t* indices,
+                                      const double* a_vals, const double* m_vals, int m_is_diag, int64_t nnz,
+                                      int nseg, const int32_t* seg_row, double sigma, int k, int block,
+                                      int max_vectors, double tol, double inner_rtol, int inner_maxiter,
+                                      uint64_t seed, double* evals, double* evecs, int32_t* status_out,
+                                      int32_t* nbasis_out, int64_t* inner_iters_out, void* ws, size_t ws_bytes,
+                                      void* stream) {
+  if (n <= 0 || !indptr || !indices || !a_vals || !m_vals || nnz <= 0 || nseg <= 0 || !seg_row || k <= 0 ||
+      !eig_block_ok(block) || !evals || !evecs || !ws || !(tol > 0) || !(inner_rtol > 0) || inner_maxiter <= 0) {
+    lapy_set_last_message("eigs_shift_invert: invalid arguments");
+    return LAPY_ERR_INVALID;
+  }
+  if (seg_row[0] != 0 || seg_row[nseg] != n) {
+    lapy_set_last_message("eigs_shift_invert: segment rows must span [0, n)");
+    return LAPY_ERR_INVALID;
+  }
+  for (int s = 0; s < nseg; ++s) {
+    const int ns = seg_row[s + 1] - seg_row[s];
+    if (ns < k + 2 * block + 1) {
+      lapy_set_last_message("eigs_shift_invert: segment %d has %d rows; need >= k + 2*block + 1 = %d", s, ns,
+                            k + 2 * block + 1);
+      return LAPY_ERR_INVALID;
+    }
+  }
+  EigPlan P;
+  plan_eig(n, nnz, nseg, seg_row, k, block, max_vectors, &P);
+  if (ws_bytes < layout_eig(P, nullptr, nullptr)) return LAPY_ERR_WORKSPACE;
+  EigPtrs e;
+  layout_eig(P, (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255)), &e);
+  EigResult r;
+  const double round_rtol = 1e-4;
+  LAPY_TRY(eigs_run(P, e, indptr, indices, a_vals, m_vals, m_is_diag, sigma, tol, inner_rtol, round_rtol,
+                    inner_maxiter, seed, evals, evecs, (cudaStream_t)stream, &r));
+  for (int s = 0; s < nseg; ++s) {
+    if (status_out) status_out[s] = r.status[s];
+    if (nbasis_out) nbasis_out[s] = r.nbasis[s];
+  }
+  if (inner_iters_out) *inner_iters_out = r.inner_iters;
+  return LAPY_OK;
+}

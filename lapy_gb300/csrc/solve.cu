@@ -1,0 +1,307 @@
+// Batched linear solves with FP64 iterative refinement around FP32 PCG.
+#include <cmath>
+#include <vector>
+#include "blas.cuh"
+#include "solve.cuh"
+#include "spmv.cuh"
+
+namespace lapy {
+
+static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t ir_workspace_bytes(int64_t n, int p, int nseg, int nchunk, int mixed, int precond) {
+  size_t b = 0;
+  b += a256(sizeof(double) * n * p);            // R64
+  b += a256(sizeof(float) * n * p) * 2;         // R32, D32
+  b += a256(sizeof(double) * nseg * p) * 2;     // bn2, rn2
+  b += a256(sizeof(int32_t) * nseg * p) * 2;    // state, mask
+  b += mixed ? pcg_workspace_bytes(n, p, nseg, nchunk, sizeof(float), precond)
+             : pcg_workspace_bytes(n, p, nseg, nchunk, sizeof(double), kPrecJacobi);
+  return b + 512;
+}
+
+__global__ void mask_cols_kernel(float* __restrict__ R, int p, const int32_t* __restrict__ chunk_row,
+                                 const int32_t* __restrict__ chunk_seg, const int32_t* __restrict__ mask) {
+  const int c = blockIdx.x;
+  const int s = chunk_seg[c];
+  const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
+  for (int64_t i = r0 * p + threadIdx.x; i < r1 * p; i += blockDim.x) {
+    const int col = (int)(i % p);
+    if (mask[s * p + col]) R[i] = 0.0f;
+  }
+}
+
+int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, double* X,
+             double rtol, int maxiter, int mixed, double inner_rtol, int max_rounds, void* ws,
+             size_t ws_bytes, cudaStream_t stream, IrStats* stats, double* relres2_host,
+             int32_t* state_host) {
+  const int64_t n = K.n;
+  const int nsp = ct.nseg * p;
+  const int precond = mixed ? K.pc32.kind : kPrecJacobi;
+  if (ws_bytes < ir_workspace_bytes(n, p, ct.nseg, ct.nchunk, mixed, precond)) return LAPY_ERR_WORKSPACE;
+  char* w = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
+  double* R64 = (double*)w; w += a256(sizeof(double) * n * p);
+  float* R32 = (float*)w; w += a256(sizeof(float) * n * p);
+  float* D32 = (float*)w; w += a256(sizeof(float) * n * p);
+  double* bn2 = (double*)w; w += a256(sizeof(double) * nsp);
+  double* rn2 = (double*)w; w += a256(sizeof(double) * nsp);
+  int32_t* st = (int32_t*)w; w += a256(sizeof(int32_t) * nsp);
+  int32_t* mask = (int32_t*)w; w += a256(sizeof(int32_t) * nsp);
+  void* pws = w;
+  const size_t pws_bytes = ws_bytes - (size_t)(w - (char*)ws);
+  const int G = spmm_pick_group(n, K.nnz);
+
+  std::vector<double> hb(nsp), hr(nsp);
+  std::vector<int32_t> hst(nsp), hmask(nsp, 0), final_st(nsp, LAPY_OK);
+  LAPY_TRY(seg_col_norm2(B, p, ct, bn2, stream));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(hb.data(), bn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
+  IrStats local;
+  if (!mixed) {
+    int it = 0;
+    PcgPrecondDesc<double> pc;
+    pc.kind = kPrecJacobi;
+    pc.dinv = K.dinv64;
+    LAPY_TRY(pcg_solve<double>(n, K.indptr, K.indices, K.k64, pc, p, ct, B, X, rtol, maxiter, st, pws,
+                               pws_bytes, stream, &it));
+    local.rounds = 1;
+    local.pcg_iters = it;
+    LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
+    LAPY_TRY(csr_spmm<double>(n, K.indptr, K.indices, K.k64, p, X, R64, -1.0, 1.0, G, stream));
+    LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
+    LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+    for (int i = 0; i < nsp; ++i) {
+      if (hst[i] < 0) final_st[i] = hst[i];
+      else if (hb[i] > 0 && !(hr[i] <= rtol * rtol * hb[i] * 1.0000001)) final_st[i] = LAPY_ERR_NOCONV;
+      if (relres2_host) relres2_host[i] = hb[i] > 0 ? hr[i] / hb[i] : 0.0;
+    }
+  } else {
+    LAPY_CUDA_TRY(cudaMemsetAsync(X, 0, sizeof(double) * n * p, stream));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
+    LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+    bool done = false;
+    for (int i = 0; i < nsp; ++i) hmask[i] = !(hb[i] > 0);
+    for (int round = 0; round < max_rounds && !done; ++round) {
+      LAPY_TRY(cast_f64_f32(n * p, R64, R32, stream));
+      if (round > 0) {
+        LAPY_CUDA_TRY(cudaMemcpyAsync(mask, hmask.data(), sizeof(int32_t) * nsp, cudaMemcpyHostToDevice, stream));
+        mask_cols_kernel<<<ct.nchunk, 256, 0, stream>>>(R32, p, ct.chunk_row, ct.chunk_seg, mask);
+        LAPY_TRY(lapy_check_launch("mask_cols_kernel"));
+      }
+      int it = 0;
+      PcgPrecondDesc<float> pc = K.pc32;
+      if (pc.kind == kPrecJacobi) pc.dinv = K.dinv32;
+      LAPY_TRY(pcg_solve<float>(n, K.indptr, K.indices, K.k32, pc, p, ct, R32, D32, inner_rtol, maxiter,
+                                st, pws, pws_bytes, stream, &it));
+      local.rounds++;
+      local.pcg_iters += it;
+      LAPY_TRY(add_f32_to_f64(n * p, D32, X, stream));
+      LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
+      LAPY_TRY(csr_spmm<double>(n, K.indptr, K.indices, K.k64, p, X, R64, -1.0, 1.0, G, stream));
+      LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
+      LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
+      LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));
+      LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+      done = true;
+      for (int i = 0; i < nsp; ++i) {
+        if (hmask[i]) continue;
+        if (hst[i] == LAPY_ERR_NAN || hst[i] == LAPY_ERR_BREAKDOWN || !std::isfinite(hr[i])) {
+          final_st[i] = (hst[i] < 0) ? hst[i] : LAPY_ERR_NAN;
+          hmask[i] = 1;
+          continue;
+        }
+        if (hr[i] <= rtol * rtol * hb[i]) hmask[i] = 1;
+        else done = false;
+      }
+    }
+    for (int i = 0; i < nsp; ++i) {
+      if (final_st[i] == LAPY_OK && hb[i] > 0 && !(hr[i] <= rtol * rtol * hb[i])) final_st[i] = LAPY_ERR_NOCONV;
+      if (relres2_host) relres2_host[i] = hb[i] > 0 ? hr[i] / hb[i] : 0.0;
+    }
+  }
+  int worst = LAPY_OK;
+  for (int i = 0; i < nsp; ++i) {
+    if (state_host) state_host[i] = final_st[i];
+    if (final_st[i] != LAPY_OK && worst == LAPY_OK) worst = final_st[i];
+  }
+  local.status = worst;
+  if (stats) *stats = local;
+  return LAPY_OK;
+}
+
+__global__ void axpby_kernel(int64_t n, double a, const double* __restrict__ x, double b,
+                             const double* __restrict__ y, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = y ? a * x[i] + b * y[i] : a * x[i];
+}
+int vec_axpby(int64_t nnz, double a, const double* x, double b, const double* y, double* out,
+              cudaStream_t stream) {
+  if (nnz <= 0) return LAPY_OK;
+  axpby_kernel<<<lapy_ceil_div(nnz, 256), 256, 0, stream>>>(nnz, a, x, b, y, out);
+  return lapy_check_launch("axpby_kernel");
+}
+
+__global__ void add_diag_kernel(int64_t n, const int32_t* __restrict__ pos, double b,
+                                const double* __restrict__ d, double* __restrict__ vals) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t k = pos[i];
+  if (k >= 0) vals[k] += b * d[i];
+}
+int add_diag(int64_t n, const int32_t* diag_pos, double b, const double* d, double* vals,
+             cudaStream_t stream) {
+  add_diag_kernel<<<lapy_ceil_div(n, 256), 256, 0, stream>>>(n, diag_pos, b, d, vals);
+  return lapy_check_launch("add_diag_kernel");
+}
+
+__global__ void jacobi_kernel(int64_t n, const int32_t* __restrict__ pos, const double* __restrict__ vals,
+                              double* __restrict__ d64, float* __restrict__ d32) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t k = pos[i];
+  const double v = (k >= 0) ? vals[k] : 0.0;
+  const double inv = (v != 0.0 && isfinite(v)) ? 1.0 / v : 1.0;
+  if (d64) d64[i] = inv;
+  if (d32) d32[i] = (float)inv;
+}
+int jacobi_inverse(int64_t n, const int32_t* diag_pos, const double* vals, double* dinv64,
+                   float* dinv32, cudaStream_t stream) {
+  jacobi_kernel<<<lapy_ceil_div(n, 256), 256, 0, stream>>>(n, diag_pos, vals, dinv64, dinv32);
+  return lapy_check_launch("jacobi_kernel");
+}
+
+}  // namespace lapy
+
+using namespace lapy;
+
+// ---------------------------------------------------------------------------
+// C ABI: element-wise matrix combination and the batched PCG solve
+// ---------------------------------------------------------------------------
+extern "C" int lapy_vec_axpby(int64_t n, double a, const double* x, double b, const double* y,
+                              double* out, void* stream) {
+  if (n < 0 || !x || !out) return LAPY_ERR_INVALID;
+  return vec_axpby(n, a, x, b, y, out, (cudaStream_t)stream);
+}
+
+extern "C" int lapy_csr_add_diag(int64_t n, const int32_t* diag_pos, double b, const double* d,
+                                 double* vals, void* stream) {
+  if (n <= 0 || !diag_pos || !d || !vals) return LAPY_ERR_INVALID;
+  return add_diag(n, diag_pos, b, d, vals, (cudaStream_t)stream);
+}
+
+static int next_pow2_le16(int c) {
+  int p = 1;
+  while (p < c && p < 16) p <<= 1;
+  return p;
+}
+
+static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed, char* base,
+                           int32_t** diag_pos, double** dinv64, float** dinv32, float** k32,
+                           double** Bp, double** Xp, void** chunk_mem, void** ir_ws, size_t* ir_bytes,
+                           int* nchunk_out, ChunkTable* ct_plan, const int32_t* seg_row) {
+  const int w = std::min(ncol, 16);
+  const int p = next_pow2_le16(w);
+  ChunkTable ct;
+  std::vector<int32_t> srow(seg_row, seg_row + nseg + 1);
+  plan_chunks(srow.data(), nseg, 4 * lapy_num_sms(), &ct);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* q = base ? base + off : nullptr;
+    off += a256(bytes);
+    return q;
+  };
+  char* p0 = take(sizeof(int32_t) * n);
+  char* p1 = take(sizeof(double) * n);
+  char* p2 = take(sizeof(float) * n);
+  char* p3 = take(sizeof(float) * nnz);
+  char* p4 = take(sizeof(double) * n * p);
+  char* p5 = take(sizeof(double) * n * p);
+  char* p6 = take(chunk_table_bytes(nseg, ct.nchunk));
+  const size_t irb = ir_workspace_bytes(n, p, nseg, ct.nchunk, mixed, kPrecJacobi);
+  char* p7 = take(irb);
+  if (base) {
+    *diag_pos = (int32_t*)p0;
+    *dinv64 = (double*)p1;
+    *dinv32 = (float*)p2;
+    *k32 = (float*)p3;
+    *Bp = (double*)p4;
+    *Xp = (double*)p5;
+    *chunk_mem = p6;
+    *ir_ws = p7;
+    *ir_bytes = irb;
+    *nchunk_out = ct.nchunk;
+    *ct_plan = ct;
+  }
+  return off + 256;
+}
+
+extern "C" size_t lapy_pcg_solve_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row,
+                                                 int ncol, int mixed) {
+  if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0) return 0;
+  return solve_layout(n, nnz, nseg, ncol, mixed, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row);
+}
+
+extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices,
+                              const double* k_vals, int64_t nnz, int nseg, const int32_t* seg_row,
+                              int ncol, const double* b, double* x, double rtol, int maxiter, int mixed,
+                              double inner_rtol, int32_t* status_out, double* relres_out,
+                              int64_t* iters_out, void* ws, size_t ws_bytes, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n <= 0 || !indptr || !indices || !k_vals || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0 ||
+      !b || !x || !(rtol > 0) || maxiter <= 0 || !ws) {
+    lapy_set_last_message("pcg_solve: invalid arguments");
+    return LAPY_ERR_INVALID;
+  }
+  if (seg_row[0] != 0 || seg_row[nseg] != n) {
+    lapy_set_last_message("pcg_solve: segment rows must span [0, n)");
+    return LAPY_ERR_INVALID;
+  }
+  if (ws_bytes < lapy_pcg_solve_workspace_bytes(n, nnz, nseg, seg_row, ncol, mixed)) return LAPY_ERR_WORKSPACE;
+  int32_t* diag_pos;
+  double *dinv64, *Bp, *Xp;
+  float *dinv32, *k32;
+  void *chunk_mem, *ir_ws;
+  size_t ir_bytes;
+  int nchunk;
+  ChunkTable ct;
+  char* base = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
+  solve_layout(n, nnz, nseg, ncol, mixed, base, &diag_pos, &dinv64, &dinv32, &k32, &Bp, &Xp, &chunk_mem,
+               &ir_ws, &ir_bytes, &nchunk, &ct, seg_row);
+  LAPY_TRY(upload_chunk_table(&ct, chunk_mem, stream));
+  LAPY_TRY(lapy_csr_diag_index(n, indptr, indices, diag_pos, stream));
+  LAPY_TRY(jacobi_inverse(n, diag_pos, k_vals, dinv64, dinv32, stream));
+  if (mixed) LAPY_TRY(cast_f64_f32(nnz, k_vals, k32, stream));
+  SysMatrix K;
+  K.n = n;
+  K.nnz = nnz;
+  K.indptr = indptr;
+  K.indices = indices;
+  K.k64 = k_vals;
+  K.k32 = k32;
+  K.dinv64 = dinv64;
+  K.dinv32 = dinv32;
+  int64_t total_iters = 0;
+  for (int c0 = 0; c0 < ncol; c0 += 16) {
+    const int w = std::min(16, ncol - c0);
+    const int p = next_pow2_le16(w);
+    LAPY_TRY(pack_cols(n, b, ncol, c0, w, p, Bp, stream));
+    std::vector<double> rr(nseg * p);
+    std::vector<int32_t> st(nseg * p);
+    IrStats stats;
+    LAPY_TRY(ir_solve(K, ct, p, Bp, Xp, rtol, maxiter, mixed, inner_rtol, 12, ir_ws, ir_bytes, stream, &stats,
+                      rr.data(), st.data()));
+    total_iters += stats.pcg_iters;
+    LAPY_TRY(unpack_cols(n, Xp, p, w, x, ncol, c0, stream));
+    for (int s = 0; s < nseg; ++s)
+      for (int c = 0; c < w; ++c) {
+        if (status_out) status_out[(int64_t)s * ncol + c0 + c] = st[s * p + c];
+        if (relres_out) relres_out[(int64_t)s * ncol + c0 + c] = std::sqrt(rr[s * p + c]);
+      }
+  }
+  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (iters_out) *iters_out = total_iters;
+  return LAPY_OK;
+}

@@ -1,0 +1,130 @@
+// CSR SpMV / SpMM with G lanes per row (G chosen from the mean row length).
+#include "spmv.cuh"
+
+namespace lapy {
+
+int spmm_pick_group(int64_t n, int64_t nnz) {
+  const double avg = n > 0 ? (double)nnz / (double)n : 1.0;
+  if (avg <= 6.0) return 4;
+  if (avg <= 12.0) return 8;
+  if (avg <= 24.0) return 16;
+  return 32;
+}
+
+template <typename V, int G, int NC>
+__global__ void __launch_bounds__(256) spmm_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                                                   const int32_t* __restrict__ indices,
+                                                   const V* __restrict__ vals, int ncol,
+                                                   const V* __restrict__ x, V* __restrict__ y,
+                                                   V alpha, V beta) {
+  const int lg = threadIdx.x & (G - 1);
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int c0 = blockIdx.y * NC;
+  const int nc = min(NC, ncol - c0);
+  const bool valid = row < n;
+  V acc[NC];
+  row_dot_group<V, V, G, NC>(indptr, indices, vals, x, ncol, c0, nc, row, valid, lg, acc);
+  if (!valid) return;
+  // lane q of the group writes column q (q < nc); for NC > G lanes loop.
+  for (int q = lg; q < nc; q += G) {
+    V v = V(0);
+#pragma unroll
+    for (int qq = 0; qq < NC; ++qq)
+      if (qq == q) v = acc[qq];
+    const int64_t o = row * ncol + c0 + q;
+    y[o] = (beta == V(0)) ? alpha * v : alpha * v + beta * y[o];
+  }
+}
+
+template <typename V, int G>
+static int launch_spmm_g(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals,
+                         int ncol, const V* x, V* y, V alpha, V beta, cudaStream_t stream) {
+  const unsigned blocks = lapy_ceil_div(n * G, 256);
+  if (ncol == 1) {
+    spmm_kernel<V, G, 1><<<dim3(blocks, 1), 256, 0, stream>>>(n, indptr, indices, vals, ncol, x, y, alpha, beta);
+  } else if (ncol <= 4) {
+    spmm_kernel<V, G, 4><<<dim3(blocks, 1), 256, 0, stream>>>(n, indptr, indices, vals, ncol, x, y, alpha, beta);
+  } else {
+    spmm_kernel<V, G, 8><<<dim3(blocks, lapy_ceil_div(ncol, 8)), 256, 0, stream>>>(n, indptr, indices, vals,
+                                                                                 ncol, x, y, alpha, beta);
+  }
+  return lapy_check_launch("spmm_kernel");
+}
+
+template <typename V>
+int csr_spmm(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals, int ncol,
+             const V* x, V* y, V alpha, V beta, int group, cudaStream_t stream) {
+  if (n <= 0 || ncol <= 0) return LAPY_OK;
+  switch (group) {
+    case 4: return launch_spmm_g<V, 4>(n, indptr, indices, vals, ncol, x, y, alpha, beta, stream);
+    case 8: return launch_spmm_g<V, 8>(n, indptr, indices, vals, ncol, x, y, alpha, beta, stream);
+    case 16: return launch_spmm_g<V, 16>(n, indptr, indices, vals, ncol, x, y, alpha, beta, stream);
+    case 32: return launch_spmm_g<V, 32>(n, indptr, indices, vals, ncol, x, y, alpha, beta, stream);
+    default: return LAPY_ERR_INVALID;
+  }
+}
+
+template int csr_spmm<double>(int64_t, const int32_t*, const int32_t*, const double*, int, const double*,
+                              double*, double, double, int, cudaStream_t);
+template int csr_spmm<float>(int64_t, const int32_t*, const int32_t*, const float*, int, const float*,
+                             float*, float, float, int, cudaStream_t);
+
+__global__ void diag_mm_kernel(int64_t n, const double* __restrict__ d, int ncol,
+                               const double* __restrict__ x, double* __restrict__ y, double alpha,
+                               double beta) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * ncol) return;
+  const double v = alpha * d[i / ncol] * x[i];
+  y[i] = (beta == 0.0) ? v : v + beta * y[i];
+}
+
+}  // namespace lapy
+
+using namespace lapy;
+
+static int spmm_args_ok(int64_t n, const int32_t* indptr, const int32_t* indices, const void* vals,
+                        int ncol, const void* x, const void* y, int group) {
+  if (n <= 0 || !indptr || !indices || !vals || ncol <= 0 || !x || !y) return 0;
+  if (group != 0 && group != 4 && group != 8 && group != 16 && group != 32) return 0;
+  if (x == y) return 0;
+  return 1;
+}
+
+extern "C" int lapy_csr_spmm_f64(int64_t n, const int32_t* indptr, const int32_t* indices,
+                                 const double* vals, int ncol, const double* x, double* y,
+                                 double alpha, double beta, int group, void* stream) {
+  if (!spmm_args_ok(n, indptr, indices, vals, ncol, x, y, group)) {
+    lapy_set_last_message("csr_spmm_f64: invalid arguments");
+    return LAPY_ERR_INVALID;
+  }
+  if (group == 0) {
+    int32_t nnz = 0;
+    LAPY_CUDA_TRY(cudaMemcpyAsync(&nnz, indptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    LAPY_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    group = spmm_pick_group(n, nnz);
+  }
+  return csr_spmm<double>(n, indptr, indices, vals, ncol, x, y, alpha, beta, group, (cudaStream_t)stream);
+}
+
+extern "C" int lapy_csr_spmm_f32(int64_t n, const int32_t* indptr, const int32_t* indices,
+                                 const float* vals, int ncol, const float* x, float* y, float alpha,
+                                 float beta, int group, void* stream) {
+  if (!spmm_args_ok(n, indptr, indices, vals, ncol, x, y, group)) {
+    lapy_set_last_message("csr_spmm_f32: invalid arguments");
+    return LAPY_ERR_INVALID;
+  }
+  if (group == 0) {
+    int32_t nnz = 0;
+    LAPY_CUDA_TRY(cudaMemcpyAsync(&nnz, indptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    LAPY_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    group = spmm_pick_group(n, nnz);
+  }
+  return csr_spmm<float>(n, indptr, indices, vals, ncol, x, y, alpha, beta, group, (cudaStream_t)stream);
+}
+
+extern "C" int lapy_diag_mm_f64(int64_t n, const double* d, int ncol, const double* x, double* y,
+                                double alpha, double beta, void* stream) {
+  if (n <= 0 || !d || ncol <= 0 || !x || !y || x == y) return LAPY_ERR_INVALID;
+  diag_mm_kernel<<<lapy_ceil_div(n * ncol, 256), 256, 0, (cudaStream_t)stream>>>(n, d, ncol, x, y, alpha, beta);
+  return lapy_check_launch("diag_mm_kernel");
+}

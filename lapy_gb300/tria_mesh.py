@@ -1,0 +1,82 @@
+"""Triangle mesh container with the members the FEM path reads.
+
+Mirrors the constructor contract of lapy/tria_mesh.py:182-280 (TriaMesh):
+vertices ``v`` (n x 3, or n x 2 padded with z = 0), triangles ``t`` (m x 3),
+the same validation errors.  Geometry work that lies on the FEM path
+(``avg_edge_length``) runs on the GPU; ``refine_`` (host-side mesh
+construction) and the curvature pre-step of the anisotropic Laplacian live in
+NumPy, as inputs to the GPU kernels.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+from scipy import sparse
+
+
+class TriaMesh:
+    """Triangle mesh (v: n x 3 float, t: m x 3 int)."""
+
+    def __init__(self, v, t, fsinfo=None):
+        self.v = np.array(v)
+        self.t = np.array(t)
+        if self.v.ndim == 2 and self.v.shape[0] < self.v.shape[1]:
+            self.v = self.v.T
+        if self.t.ndim == 2 and self.t.shape[1] != 3 and self.t.shape[0] == 3:
+            self.t = self.t.T
+        if self.t.size == 0:
+            raise ValueError("Mesh has no triangles (empty mesh)")
+        if self.v.size == 0:
+            raise ValueError("Mesh has no vertices (empty mesh)")
+        vnum = np.max(self.v.shape)
+        if np.max(self.t) >= vnum:
+            raise ValueError("Max index exceeds number of vertices")
+        if self.t.shape[1] != 3:
+            raise ValueError("Triangles should have 3 vertices")
+        if self.v.shape[1] == 2:
+            self.v = np.column_stack([self.v, np.zeros(self.v.shape[0], dtype=self.v.dtype)])
+            self._is_2d = True
+        elif self.v.shape[1] == 3:
+            self._is_2d = False
+        else:
+            raise ValueError("Vertices should have 2 or 3 coordinates")
+        self.fsinfo = fsinfo
+
+    def is_2d(self) -> bool:
+        return self._is_2d
+
+    # -- host-side adjacency (mesh construction only) ---------------------
+    def _adj_sym(self) -> sparse.csc_matrix:
+        t0, t1, t2 = self.t[:, 0], self.t[:, 1], self.t[:, 2]
+        i = np.column_stack((t0, t1, t1, t2, t2, t0)).reshape(-1)
+        j = np.column_stack((t1, t0, t2, t1, t0, t2)).reshape(-1)
+        n = self.v.shape[0]
+        return sparse.csc_matrix((np.ones(i.shape), (i, j)), shape=(n, n))
+
+    def avg_edge_length(self) -> float:
+        """Mean edge length (lapy/tria_mesh.py:735-748), computed on the GPU."""
+        from ._geometry import avg_edge_length
+
+        return avg_edge_length(self)
+
+    def refine_(self, it: int = 1) -> None:
+        """1-to-4 midpoint subdivision (lapy/tria_mesh.py:1452-1487).
+
+        New vertices are numbered after the old ones in row-major order of the
+        upper-triangular edge list; each parent triangle (a, b, c) with edge
+        midpoints ab, bc, ca becomes (a, ab, ca), (b, bc, ab), (c, ca, bc),
+        (ab, bc, ca), in that order.
+        """
+        for _ in range(it):
+            adj = sparse.triu(self._adj_sym(), 0, format="csr")
+            vno = self.v.shape[0]
+            rows, cols = adj.nonzero()
+            eid = sparse.csr_matrix((np.arange(vno, vno + rows.size), (rows, cols)), shape=adj.shape)
+            eid = (eid + eid.T).tocsr()
+            vnew = np.append(self.v, 0.5 * (self.v[rows, :] + self.v[cols, :]), axis=0)
+            t = self.t
+            e1 = np.asarray(eid[t[:, 0], t[:, 1]]).ravel()
+            e2 = np.asarray(eid[t[:, 1], t[:, 2]]).ravel()
+            e3 = np.asarray(eid[t[:, 2], t[:, 0]]).ravel()
+            tnew = np.column_stack((t[:, 0], e1, e3, t[:, 1], e2, e1, t[:, 2], e3, e2, e1, e2, e3)).reshape(-1, 3)
+            self.__init__(vnew, tnew, self.fsinfo)
