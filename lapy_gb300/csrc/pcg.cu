@@ -1,11 +1,10 @@
 // Persistent cooperative PCG over a block-diagonal batch of CSR systems.
 //
 // One launch runs the whole solve.  Rows are split into chunks that never
-// cross a segment (one mesh = one segment); every CTA owns a contiguous range
-// of chunks.  Dot products are per (segment, column): each chunk writes its
+// cross a segment (one mesh = one segment).  Dot products are per (segment, column): each chunk writes its
 // partial sum, and after a grid barrier every CTA that needs a segment's
 // scalar re-reduces that segment's partials in a fixed order, so the result
-// is bitwise reproducible.  Three barriers per iteration (Jacobi), five with
+// is bitwise reproducible.  Chunks are dealt to CTAs round-robin.  Three barriers per iteration (Jacobi), five with
 // the factored preconditioner z = Gt (G r).  Convergence is tracked per
 // (segment, column); converged columns freeze and fully converged segments
 // skip their rows.  Barriers spin with a bound (common.cuh).
@@ -19,11 +18,13 @@ namespace lapy {
 
 constexpr int32_t kActive = INT32_MAX;
 constexpr int kPcgThreads = 256;
+// staged nonzeros per tile (values + column indices in shared memory)
+constexpr int kStageCap = 3072;
 
 int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable* ct) {
   const int64_t total = seg_row[nseg] - seg_row[0];
   int64_t cr = (total + std::max(1, target_chunks) - 1) / std::max(1, target_chunks);
-  cr = std::max<int64_t>(32, std::min<int64_t>(4096, cr));
+  cr = std::max<int64_t>(32, std::min<int64_t>(1024, cr));
   cr = (cr + 31) / 32 * 32;
   ct->nseg = nseg;
   ct->h_seg_row.assign(seg_row, seg_row + nseg + 1);
@@ -153,25 +154,17 @@ __device__ __forceinline__ void cta_partial_store(double acc, PcgShared<NP>& sh,
   __syncthreads();
 }
 
-// Per-group partial for SpMM outputs: lane lg owns columns lg, lg+G, ...
-template <int NP, int G>
-__device__ __forceinline__ void cta_group_partial_store(double (&acc)[(NP + G - 1) / G],
-                                                        PcgShared<NP>& sh, double* dst) {
+// Reduce per-thread partials of all NP columns (one row per thread) and store
+// them to dst[0..NP).
+template <int NP>
+__device__ __forceinline__ void cta_rows_partial_store(const double (&acc)[NP], PcgShared<NP>& sh,
+                                                       double* dst) {
   const int t = threadIdx.x;
-  const int lane = t & 31, lg = t & (G - 1);
-  constexpr int NPL = (NP + G - 1) / G;
-#pragma unroll
-  for (int j = 0; j < NPL; ++j) {
-#pragma unroll
-    for (int o = 16; o >= G; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
-  }
   __syncthreads();
-  if (lane < G) {
 #pragma unroll
-    for (int j = 0; j < NPL; ++j) {
-      const int q = lg + j * G;
-      if (q < NP) sh.red[t >> 5][q] = acc[j];
-    }
+  for (int q = 0; q < NP; ++q) {
+    const double v = warp_sum(acc[q]);
+    if ((t & 31) == 0) sh.red[t >> 5][q] = v;
   }
   __syncthreads();
   if (t < NP) {
@@ -183,55 +176,123 @@ __device__ __forceinline__ void cta_group_partial_store(double (&acc)[(NP + G - 
   __syncthreads();
 }
 
-// Y[rows of chunk] = Mat * Xin for NP columns (G lanes per row); optionally
-// accumulate sum_rows Wdot[row,q] * Y[row,q] into `dacc`.
-template <typename V, int NP, int G, bool DOT>
+// NP consecutive values of row `row` (vectorised: rows are NP * sizeof(V)
+// aligned because every buffer starts on a 256-byte boundary).
+template <typename V, int NP>
+__device__ __forceinline__ void load_row(const V* __restrict__ base, int64_t row, V (&out)[NP]) {
+  const V* p = base + row * NP;
+  if constexpr (sizeof(V) == 4 && NP % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < NP / 4; ++j) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(p) + j);
+      out[4 * j] = v.x; out[4 * j + 1] = v.y; out[4 * j + 2] = v.z; out[4 * j + 3] = v.w;
+    }
+  } else if constexpr (sizeof(V) == 4 && NP == 2) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    out[0] = v.x; out[1] = v.y;
+  } else if constexpr (sizeof(V) == 8 && NP % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < NP / 2; ++j) {
+      const double2 v = __ldg(reinterpret_cast<const double2*>(p) + j);
+      out[2 * j] = v.x; out[2 * j + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < NP; ++j) out[j] = p[j];
+  }
+}
+
+template <typename V, int NP>
+__device__ __forceinline__ void store_row(V* __restrict__ base, int64_t row, const V (&v)[NP]) {
+  V* p = base + row * NP;
+  if constexpr (sizeof(V) == 4 && NP % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < NP / 4; ++j)
+      reinterpret_cast<float4*>(p)[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+  } else if constexpr (sizeof(V) == 4 && NP == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  } else if constexpr (sizeof(V) == 8 && NP % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < NP / 2; ++j) reinterpret_cast<double2*>(p)[j] = make_double2(v[2 * j], v[2 * j + 1]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < NP; ++j) p[j] = v[j];
+  }
+}
+
+// Shared-memory-staged SpMM over the rows [r0, r1) of one chunk: tiles of
+// kPcgThreads rows; the tile's contiguous slice of values and column indices
+// is first copied into shared memory with coalesced loads (every thread keeps
+// several independent loads in flight), then each thread forms one row,
+// gathering the NP-wide rows of Xin.  Tiles longer than the staging buffer
+// read the matrix directly.  With DOT, dacc[q] += Wdot(row, q) * Y(row, q).
+template <typename V, int NP, bool DOT>
 __device__ __forceinline__ void chunk_spmm(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                                            const V* __restrict__ val, const V* __restrict__ Xin,
                                            V* __restrict__ Y, const V* __restrict__ Wdot, int r0, int r1,
-                                           double (&dacc)[(NP + G - 1) / G]) {
-  const int lg = threadIdx.x & (G - 1);
-  constexpr int RPP = kPcgThreads / G;
-  const int npass = (r1 - r0 + RPP - 1) / RPP;
-  for (int k = 0; k < npass; ++k) {
-    const int row = r0 + k * RPP + threadIdx.x / G;
-    const bool valid = row < r1;
-    V acc[NP];
-    row_dot_group<V, V, G, NP>(ptr, idx, val, Xin, NP, 0, NP, row, valid, lg, acc);
-    if (valid) {
+                                           V* __restrict__ sval, int32_t* __restrict__ sidx,
+                                           double (&dacc)[NP]) {
+  const int t = threadIdx.x;
+  for (int tr0 = r0; tr0 < r1; tr0 += kPcgThreads) {
+    const int tr1 = min(tr0 + kPcgThreads, r1);
+    const int32_t k0 = ptr[tr0], k1 = ptr[tr1];
+    const bool staged = (k1 - k0) <= kStageCap;
+    __syncthreads();  // the previous tile is done with the staging buffer
+    if (staged) {
+      for (int32_t e = t; e < k1 - k0; e += kPcgThreads) {
+        sval[e] = val[k0 + e];
+        sidx[e] = idx[k0 + e];
+      }
+    }
+    __syncthreads();
+    const int row = tr0 + t;
+    if (row < tr1) {
+      const int32_t kb = ptr[row], ke = ptr[row + 1];
+      V acc[NP];
 #pragma unroll
-      for (int j = 0; j < (NP + G - 1) / G; ++j) {
-        const int q = lg + j * G;
-        if (q < NP) {
-          V v = V(0);
+      for (int q = 0; q < NP; ++q) acc[q] = V(0);
+#pragma unroll 4
+      for (int32_t k = kb; k < ke; ++k) {
+        const V a = staged ? sval[k - k0] : val[k];
+        const int32_t c = staged ? sidx[k - k0] : idx[k];
+        V xr[NP];
+        load_row<V, NP>(Xin, c, xr);
 #pragma unroll
-          for (int qq = 0; qq < NP; ++qq)
-            if (qq == q) v = acc[qq];
-          Y[(int64_t)row * NP + q] = v;
-          if (DOT) dacc[j] += (double)Wdot[(int64_t)row * NP + q] * (double)v;
-        }
+        for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
+      }
+      store_row<V, NP>(Y, row, acc);
+      if (DOT) {
+        V w[NP];
+        load_row<V, NP>(Wdot, row, w);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) dacc[q] += (double)(w[q] * acc[q]);
       }
     }
   }
 }
 
-template <typename V, int NP, int G, int PC>
+template <typename V, int NP, int PC>
 __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   __shared__ PcgShared<NP> sh;
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  V* sval = reinterpret_cast<V*>(stage_raw);
+  int32_t* sidx = reinterpret_cast<int32_t*>(stage_raw + sizeof(V) * kStageCap);
   const int t = threadIdx.x;
-  const int c_begin = (int)((int64_t)blockIdx.x * a.nchunk / gridDim.x);
-  const int c_end = (int)((int64_t)(blockIdx.x + 1) * a.nchunk / gridDim.x);
+  // Chunks are dealt round-robin: every CTA holds pieces of many segments,
+  // so the work stays balanced while segments converge at different times.
+  const int c_begin = blockIdx.x, c_step = gridDim.x;
+  const int c_end = a.nchunk;
   double* part_pq = a.part;
   double* part_rz = a.part + (int64_t)a.nchunk * NP;
   double* part_rr = a.part + 2 * (int64_t)a.nchunk * NP;
   const int colt = t % NP;  // fixed column of this thread in element-wise loops
-  constexpr int NPL = (NP + G - 1) / G;
+  constexpr int U = 4;      // element-wise unroll: U independent streams per thread
 
   // ---- phase 0: X = 0, R = B, Z = M^-1 R, P = Z; partial b'b and r'z
-  for (int c = c_begin; c < c_end; ++c) {
-    const int r0 = a.chunk_row[c], r1 = a.chunk_row[c + 1];
+  for (int c = c_begin; c < c_end; c += c_step) {
+    const int64_t e0 = (int64_t)a.chunk_row[c] * NP, e1 = (int64_t)a.chunk_row[c + 1] * NP;
     double bb = 0.0, rz = 0.0;
-    for (int64_t i = (int64_t)r0 * NP + t; i < (int64_t)r1 * NP; i += kPcgThreads) {
+    for (int64_t i = e0 + t; i < e1; i += kPcgThreads) {
       const V b = a.B[i];
       a.X[i] = V(0);
       a.R[i] = b;
@@ -247,28 +308,28 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   }
   if (PC == kPrecFactored) {
     if (!grid_sync(a.bar)) return;
-    double dummy[NPL];
-    for (int c = c_begin; c < c_end; ++c)
-      chunk_spmm<V, NP, G, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr,
-                                  a.chunk_row[c], a.chunk_row[c + 1], dummy);
+    double dummy[NP];
+    for (int c = c_begin; c < c_end; c += c_step)
+      chunk_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.chunk_row[c],
+                               a.chunk_row[c + 1], sval, sidx, dummy);
     if (!grid_sync(a.bar)) return;
-    for (int c = c_begin; c < c_end; ++c) {
-      double acc[NPL];
+    for (int c = c_begin; c < c_end; c += c_step) {
+      double acc[NP];
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) acc[j] = 0.0;
-      chunk_spmm<V, NP, G, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R,
-                                 a.chunk_row[c], a.chunk_row[c + 1], acc);
-      cta_group_partial_store<NP, G>(acc, sh, part_rz + (int64_t)c * NP);
+      for (int j = 0; j < NP; ++j) acc[j] = 0.0;
+      chunk_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R, a.chunk_row[c],
+                              a.chunk_row[c + 1], sval, sidx, acc);
+      cta_rows_partial_store<NP>(acc, sh, part_rz + (int64_t)c * NP);
     }
     if (!grid_sync(a.bar)) return;
-    for (int c = c_begin; c < c_end; ++c) {
-      const int r0 = a.chunk_row[c], r1 = a.chunk_row[c + 1];
-      for (int64_t i = (int64_t)r0 * NP + t; i < (int64_t)r1 * NP; i += kPcgThreads) a.P[i] = a.Z[i];
+    for (int c = c_begin; c < c_end; c += c_step) {
+      const int64_t e0 = (int64_t)a.chunk_row[c] * NP, e1 = (int64_t)a.chunk_row[c + 1] * NP;
+      for (int64_t i = e0 + t; i < e1; i += kPcgThreads) a.P[i] = a.Z[i];
     }
   }
   if (!grid_sync(a.bar)) return;
   // ---- segment initialisation (first chunk of each segment publishes)
-  for (int c = c_begin; c < c_end; ++c) {
+  for (int c = c_begin; c < c_end; c += c_step) {
     const int s = a.chunk_seg[c];
     if (a.seg_chunk[s] != c) continue;
     seg_reduce<NP>(part_rr, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s0);
@@ -301,9 +362,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
 
     // ---- phase A: Q = K P, partial p'q
     if (blockIdx.x == 0 && t == 0) a.active[par ^ 1] = 0u;
-    sh.seg = -1;
+    if (t == 0) sh.seg = -1;
     __syncthreads();
-    for (int c = c_begin; c < c_end; ++c) {
+    for (int c = c_begin; c < c_end; c += c_step) {
       const int s = a.chunk_seg[c];
       if (s != sh.seg) {
         __syncthreads();
@@ -319,12 +380,12 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
         if (t < NP) part_pq[(int64_t)c * NP + t] = 0.0;
         continue;
       }
-      double acc[NPL];
+      double acc[NP];
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) acc[j] = 0.0;
-      chunk_spmm<V, NP, G, true>(a.indptr, a.indices, a.vals, a.P, a.Q, a.P, a.chunk_row[c],
-                                 a.chunk_row[c + 1], acc);
-      cta_group_partial_store<NP, G>(acc, sh, part_pq + (int64_t)c * NP);
+      for (int j = 0; j < NP; ++j) acc[j] = 0.0;
+      chunk_spmm<V, NP, true>(a.indptr, a.indices, a.vals, a.P, a.Q, a.P, a.chunk_row[c], a.chunk_row[c + 1],
+                              sval, sidx, acc);
+      cta_rows_partial_store<NP>(acc, sh, part_pq + (int64_t)c * NP);
       if (t == 0) {
         const int r0 = a.chunk_row[c], r1 = a.chunk_row[c + 1];
         atomicAdd(&a.work[0], (unsigned long long)(r1 - r0));
@@ -334,9 +395,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
     if (!grid_sync(a.bar)) return;
 
     // ---- phase B: alpha, X += alpha P, R -= alpha Q, partial r'r (and r'z for Jacobi)
-    sh.seg = -1;
+    if (t == 0) sh.seg = -1;
     __syncthreads();
-    for (int c = c_begin; c < c_end; ++c) {
+    for (int c = c_begin; c < c_end; c += c_step) {
       const int s = a.chunk_seg[c];
       if (s != sh.seg) {
         seg_reduce<NP>(part_pq, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s0);
@@ -356,7 +417,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
         }
         __syncthreads();
       }
-      const int r0 = a.chunk_row[c], r1 = a.chunk_row[c + 1];
+      const int64_t e0 = (int64_t)a.chunk_row[c] * NP, e1 = (int64_t)a.chunk_row[c + 1] * NP;
       if (!sh.any) {
         if (t < NP) {
           part_rr[(int64_t)c * NP + t] = 0.0;
@@ -366,44 +427,60 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
       }
       const V alpha = (V)sh.scal[colt];
       const bool act = sh.act[colt];
-      double rr = 0.0, rz = 0.0;
-      for (int64_t i = (int64_t)r0 * NP + t; i < (int64_t)r1 * NP; i += kPcgThreads) {
-        V r = a.R[i];
-        if (act) {
-          a.X[i] = a.X[i] + alpha * a.P[i];
-          r = r - alpha * a.Q[i];
-          a.R[i] = r;
+      float rr = 0.f, rz = 0.f;
+      for (int64_t i0 = e0 + t; i0 < e1; i0 += U * kPcgThreads) {
+        V xv[U], pv[U], qv[U], rv[U], dv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int64_t i = i0 + u * kPcgThreads;
+          if (i < e1) {
+            rv[u] = a.R[i];
+            if (act) { xv[u] = a.X[i]; pv[u] = a.P[i]; qv[u] = a.Q[i]; }
+            if (PC == kPrecJacobi) dv[u] = a.pc.dinv[i / NP];
+          }
         }
-        rr += (double)r * (double)r;
-        if (PC == kPrecJacobi) rz += (double)r * (double)(a.pc.dinv[i / NP] * r);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int64_t i = i0 + u * kPcgThreads;
+          if (i < e1) {
+            V r = rv[u];
+            if (act) {
+              a.X[i] = xv[u] + alpha * pv[u];
+              r = r - alpha * qv[u];
+              a.R[i] = r;
+            }
+            rr += (float)(r * r);
+            if (PC == kPrecJacobi) rz += (float)(r * (dv[u] * r));
+          }
+        }
       }
-      cta_partial_store<NP>(rr, sh, part_rr + (int64_t)c * NP);
-      if (PC == kPrecJacobi) cta_partial_store<NP>(rz, sh, part_rz + (int64_t)c * NP);
+      cta_partial_store<NP>((double)rr, sh, part_rr + (int64_t)c * NP);
+      if (PC == kPrecJacobi) cta_partial_store<NP>((double)rz, sh, part_rz + (int64_t)c * NP);
     }
     if (!grid_sync(a.bar)) return;
 
     if (PC == kPrecFactored) {
       // ---- phase B2: T = G R ; phase B3: Z = Gt T, partial r'z
-      double dummy[NPL];
-      for (int c = c_begin; c < c_end; ++c)
-        chunk_spmm<V, NP, G, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr,
-                                    a.chunk_row[c], a.chunk_row[c + 1], dummy);
+      double dummy[NP];
+      for (int c = c_begin; c < c_end; c += c_step)
+        chunk_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.chunk_row[c],
+                                 a.chunk_row[c + 1], sval, sidx, dummy);
       if (!grid_sync(a.bar)) return;
-      for (int c = c_begin; c < c_end; ++c) {
-        double acc[NPL];
+      for (int c = c_begin; c < c_end; c += c_step) {
+        double acc[NP];
 #pragma unroll
-        for (int j = 0; j < NPL; ++j) acc[j] = 0.0;
-        chunk_spmm<V, NP, G, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R,
-                                   a.chunk_row[c], a.chunk_row[c + 1], acc);
-        cta_group_partial_store<NP, G>(acc, sh, part_rz + (int64_t)c * NP);
+        for (int j = 0; j < NP; ++j) acc[j] = 0.0;
+        chunk_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R, a.chunk_row[c],
+                                a.chunk_row[c + 1], sval, sidx, acc);
+        cta_rows_partial_store<NP>(acc, sh, part_rz + (int64_t)c * NP);
       }
       if (!grid_sync(a.bar)) return;
     }
 
     // ---- phase C: convergence, beta, P = Z + beta P
-    sh.seg = -1;
+    if (t == 0) sh.seg = -1;
     __syncthreads();
-    for (int c = c_begin; c < c_end; ++c) {
+    for (int c = c_begin; c < c_end; c += c_step) {
       const int s = a.chunk_seg[c];
       if (s != sh.seg) {
         seg_reduce<NP>(part_pq, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s0);
@@ -422,7 +499,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
           const bool act = st == kActive;
           sh.scal[t] = act ? rzn / rz_cur[s * NP + t] : 0.0;
           sh.act[t] = act;
-          if (a.seg_chunk[s] == c) {
+          if (a.seg_chunk[s] == c) {  // a segment's first chunk always starts a new run
             st_nxt[s * NP + t] = st;
             rz_nxt[s * NP + t] = rzn;
             if (act) atomicAdd(&a.active[par ^ 1], 1u);
@@ -436,17 +513,26 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
           sh.any = any;
         }
         __syncthreads();
-      } else if (a.seg_chunk[s] == c) {
-        // (a segment's first chunk always starts a new segment run)
       }
       if (!sh.any) continue;
-      const int r0 = a.chunk_row[c], r1 = a.chunk_row[c + 1];
+      const int64_t e0 = (int64_t)a.chunk_row[c] * NP, e1 = (int64_t)a.chunk_row[c + 1] * NP;
       const V beta = (V)sh.scal[colt];
-      const bool act = sh.act[colt];
-      if (act) {
-        for (int64_t i = (int64_t)r0 * NP + t; i < (int64_t)r1 * NP; i += kPcgThreads) {
-          const V z = (PC == kPrecJacobi) ? a.pc.dinv[i / NP] * a.R[i] : a.Z[i];
-          a.P[i] = z + beta * a.P[i];
+      if (sh.act[colt]) {
+        for (int64_t i0 = e0 + t; i0 < e1; i0 += U * kPcgThreads) {
+          V zv[U], pv[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int64_t i = i0 + u * kPcgThreads;
+            if (i < e1) {
+              zv[u] = (PC == kPrecJacobi) ? a.pc.dinv[i / NP] * a.R[i] : a.Z[i];
+              pv[u] = a.P[i];
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int64_t i = i0 + u * kPcgThreads;
+            if (i < e1) a.P[i] = zv[u] + beta * pv[u];
+          }
         }
       }
     }
@@ -456,7 +542,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   // ---- publish the final state (first chunk of each segment)
   const int par = it & 1;
   const int32_t* st_cur = a.state + par * (int64_t)a.nseg * NP;
-  for (int c = c_begin; c < c_end; ++c) {
+  for (int c = c_begin; c < c_end; c += c_step) {
     const int s = a.chunk_seg[c];
     if (a.seg_chunk[s] != c) continue;
     if (t < NP) {
@@ -479,38 +565,30 @@ size_t pcg_workspace_bytes(int64_t n, int p, int nseg, int nchunk, int elem_size
   return b + 256;
 }
 
-template <typename V, int NP, int G, int PC>
+template <typename V, int NP, int PC>
 static int launch_pcg(PcgArgs<V>& args, cudaStream_t stream) {
-  auto kern = pcg_kernel<V, NP, G, PC>;
+  auto kern = pcg_kernel<V, NP, PC>;
+  const size_t smem = (sizeof(V) + sizeof(int32_t)) * kStageCap;
   int per_sm = 0;
-  LAPY_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPcgThreads, 0));
+  LAPY_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPcgThreads, smem));
   if (per_sm <= 0) {
     lapy_set_last_message("pcg: kernel cannot be resident (occupancy 0)");
     return LAPY_ERR_CUDA;
   }
   const int grid = std::max(1, std::min(per_sm * lapy_num_sms(), args.nchunk));
   void* kargs[] = {(void*)&args};
-  LAPY_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kPcgThreads), kargs, 0, stream));
+  LAPY_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kPcgThreads), kargs, smem, stream));
   return lapy_check_launch("pcg_kernel");
 }
 
-template <typename V, int NP, int PC>
-static int launch_pcg_g(PcgArgs<V>& args, int G, cudaStream_t stream) {
-  switch (G) {
-    case 4: return launch_pcg<V, NP, 4, PC>(args, stream);
-    case 8: return launch_pcg<V, NP, 8, PC>(args, stream);
-    default: return launch_pcg<V, NP, 16, PC>(args, stream);
-  }
-}
-
 template <typename V, int PC>
-static int launch_pcg_np(PcgArgs<V>& args, int p, int G, cudaStream_t stream) {
+static int launch_pcg_np(PcgArgs<V>& args, int p, cudaStream_t stream) {
   switch (p) {
-    case 1: return launch_pcg_g<V, 1, PC>(args, G, stream);
-    case 2: return launch_pcg_g<V, 2, PC>(args, G, stream);
-    case 4: return launch_pcg_g<V, 4, PC>(args, G, stream);
-    case 8: return launch_pcg_g<V, 8, PC>(args, G, stream);
-    case 16: return launch_pcg_g<V, 16, PC>(args, G, stream);
+    case 1: return launch_pcg<V, 1, PC>(args, stream);
+    case 2: return launch_pcg<V, 2, PC>(args, stream);
+    case 4: return launch_pcg<V, 4, PC>(args, stream);
+    case 8: return launch_pcg<V, 8, PC>(args, stream);
+    case 16: return launch_pcg<V, 16, PC>(args, stream);
     default:
       lapy_set_last_message("pcg: block width %d not in {1,2,4,8,16}", p);
       return LAPY_ERR_INVALID;
@@ -563,9 +641,6 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
   a.rtol2 = rtol * rtol;
   a.maxiter = maxiter;
   LAPY_CUDA_TRY(cudaMemsetAsync(ctl, 0, 64, stream));
-  const int64_t nnz_est = 7 * n;
-  (void)nnz_est;
-  const int G = 8;
   int st;
   const bool prof = lapy_profile_enabled();
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -575,9 +650,9 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
     LAPY_CUDA_TRY(cudaEventRecord(e0, stream));
   }
   if (pc.kind == kPrecFactored)
-    st = launch_pcg_np<V, kPrecFactored>(a, p, G, stream);
+    st = launch_pcg_np<V, kPrecFactored>(a, p, stream);
   else
-    st = launch_pcg_np<V, kPrecJacobi>(a, p, G, stream);
+    st = launch_pcg_np<V, kPrecJacobi>(a, p, stream);
   if (st != LAPY_OK) return st;
   if (prof) LAPY_CUDA_TRY(cudaEventRecord(e1, stream));
   unsigned hctl[10];

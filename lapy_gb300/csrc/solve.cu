@@ -82,6 +82,9 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
     LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
     bool done = false;
     for (int i = 0; i < nsp; ++i) hmask[i] = !(hb[i] > 0);
+    // per-round FP32 target: at least inner_rtol, but only the reduction still
+    // missing (with a factor 4 margin) once the residual is close to rtol
+    double round_rtol = inner_rtol;
     for (int round = 0; round < max_rounds && !done; ++round) {
       LAPY_TRY(cast_f64_f32(n * p, R64, R32, stream));
       if (round > 0) {
@@ -92,7 +95,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
       int it = 0;
       PcgPrecondDesc<float> pc = K.pc32;
       if (pc.kind == kPrecJacobi) pc.dinv = K.dinv32;
-      LAPY_TRY(pcg_solve<float>(n, K.indptr, K.indices, K.k32, pc, p, ct, R32, D32, inner_rtol, maxiter,
+      LAPY_TRY(pcg_solve<float>(n, K.indptr, K.indices, K.k32, pc, p, ct, R32, D32, round_rtol, maxiter,
                                 st, pws, pws_bytes, stream, &it));
       local.rounds++;
       local.pcg_iters += it;
@@ -114,6 +117,10 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
         if (hr[i] <= rtol * rtol * hb[i]) hmask[i] = 1;
         else done = false;
       }
+      double need = 1.0;  // largest remaining reduction factor over active columns
+      for (int i = 0; i < nsp; ++i)
+        if (!hmask[i] && hr[i] > 0) need = std::min(need, 0.25 * rtol * std::sqrt(hb[i] / hr[i]));
+      round_rtol = std::max(inner_rtol, std::min(0.5, need));
     }
     for (int i = 0; i < nsp; ++i) {
       if (final_st[i] == LAPY_OK && hb[i] > 0 && !(hr[i] <= rtol * rtol * hb[i])) final_st[i] = LAPY_ERR_NOCONV;

@@ -137,8 +137,8 @@ class Solver:
             return A, M.data.contiguous(), False
         return A, M.on_pattern(A.indptr, A.indices, A.data.numel()), False
 
-    def eigs(self, k: int = 10, sigma: float = -0.01, block: int | None = None, tol: float = 1e-10,
-             inner_rtol: float = 1e-8):
+    def eigs(self, k: int = 10, sigma: float = -0.01, block: int | None = None, tol: float = 1e-8,
+             inner_rtol: float = 1e-9):
         """The k eigenpairs of A x = lambda M x nearest ``sigma`` (ascending)."""
         A, mvals, m_diag = self._device_pair()
         n = A.n
@@ -156,6 +156,20 @@ class Solver:
         return evals[0].cpu().numpy(), evecs.cpu().numpy()
 
     # -- Poisson ---------------------------------------------------------------
+    def _masked_solve(self, A: DeviceCSR, b: torch.Tensor, mask: np.ndarray, rtol: float) -> torch.Tensor:
+        """Solve A x = b with the rows/columns of masked vertices replaced by
+        identity rows (their entries of b zeroed): the reduced system
+        A[free][:, free] of lapy/solver.py:848-865 without forming it."""
+        L = _lib.lib()
+        maskd = torch.from_numpy(mask).to("cuda")
+        kv = torch.empty_like(A.data.double())
+        _lib.check(L.lapy_csr_dirichlet_mask(A.n, dptr(A.indptr), dptr(A.indices), dptr(A.data.double().contiguous()),
+                                             dptr(maskd), dptr(kv), stream()), "csr_dirichlet_mask")
+        b = b.clone()
+        b[maskd.bool()] = 0.0
+        x, _, _ = pcg_solve(A.indptr, A.indices, kv, A.n, kv.numel(), b, rtol)
+        return x
+
     def poisson(self, h=0.0, dtup=(), ntup=(), rtol: float = 1e-12):
         """Poisson equation A x = M (h - n) with Dirichlet/Neumann data (lapy/solver.py:718-889)."""
         dim = self._A.n
@@ -212,20 +226,19 @@ class Solver:
             b = b - A.matmul(Dd)
             mask = np.zeros(dim, dtype=np.uint8)
             mask[didx] = 1
-            maskd = torch.from_numpy(mask).to("cuda")
-            kv = torch.empty_like(A.data.double())
-            _lib.check(L.lapy_csr_dirichlet_mask(dim, dptr(A.indptr), dptr(A.indices), dptr(A.data.double().contiguous()),
-                                                 dptr(maskd), dptr(kv), stream()), "csr_dirichlet_mask")
-            b[maskd.bool()] = 0.0
-            x, relres, _ = pcg_solve(A.indptr, A.indices, kv, dim, kv.numel(), b, rtol)
-            x[maskd.bool()] = Dd[maskd.bool()]
+            x = self._masked_solve(A, b, mask, rtol)
+            md = torch.from_numpy(mask).to("cuda").bool()
+            x[md] = Dd[md]
         else:
-            # Neumann everywhere: A is singular (constants span its kernel).  The
-            # reference's LU returns one solution with an arbitrary constant; here
-            # b is made consistent (mean removed) and the zero-mean solution is
-            # returned.
+            # Neumann everywhere: A is singular (constants span its kernel on a
+            # connected mesh).  The reference's LU returns one solution with an
+            # arbitrary constant.  Here b is made consistent (mean removed), one
+            # vertex is pinned to 0, which leaves an SPD system with the same
+            # solutions up to a constant, and the zero-mean solution is returned.
             b = b - b.mean(dim=0, keepdim=True)
-            x, relres, _ = pcg_solve(A.indptr, A.indices, A.data.double().contiguous(), dim, A.data.numel(), b, rtol)
+            mask = np.zeros(dim, dtype=np.uint8)
+            mask[0] = 1
+            x = self._masked_solve(A, b, mask, rtol)
             x = x - x.mean(dim=0, keepdim=True)
         x = x.cpu().numpy().astype(dtype, copy=False)
         if scalar_rhs:
@@ -234,7 +247,7 @@ class Solver:
 
 
 def eigs_batched(indptr, indices, a_vals, m_vals, m_is_diag: bool, seg_row, k: int, sigma: float = -0.01,
-                 block: int = DEFAULT_BLOCK, tol: float = 1e-10, inner_rtol: float = 1e-8, inner_maxiter: int = 20000,
+                 block: int = DEFAULT_BLOCK, tol: float = 1e-8, inner_rtol: float = 1e-9, inner_maxiter: int = 20000,
                  max_vectors: int | None = None, seed: int = 1234):
     """Shift-invert eigenpairs of every segment of a block-diagonal batch.
 

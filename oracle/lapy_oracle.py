@@ -304,19 +304,38 @@ def normalize_rows(g, scaled=True):
     return np.nan_to_num(out)
 
 
-def geodesic_f(v, t, u, scaled=True):
+def poisson_neumann_consistent(A, b):
+    """Solution of the singular Neumann system A x = b on a connected mesh:
+    the part of b along the constants is removed (making it consistent), one
+    vertex is pinned to 0 and the reduced SPD system is solved by splu.  The
+    reference instead factors the singular A (solver.py:873-877), whose result
+    carries the inconsistent part of b amplified by the near-zero pivot."""
+    b = np.asarray(b, dtype=np.float64)
+    b = b - b.mean(axis=0)
+    mask = np.ones(A.shape[0], dtype=bool)
+    mask[0] = False
+    Af = sparse.csc_matrix(A)[:, mask].tocsr()[mask, :].tocsc()
+    x = np.zeros_like(b)
+    x[mask] = splu(Af).solve(b[mask])
+    return x
+
+
+def geodesic_f(v, t, u, scaled=True, consistent=False):
     """compute_geodesic_f (diffgeo.py:144-165): gradient, normalise, divergence,
-    Poisson with the identity mass, minus the minimum."""
+    Poisson with the identity mass, minus the minimum.  ``consistent`` solves
+    the singular Poisson problem with poisson_neumann_consistent."""
     npe = t.shape[1]
     grad = tria_gradient(v, t, u) if npe == 3 else tet_gradient(v, t, u)
     gn = normalize_rows(grad, scaled)
     div = tria_divergence(v, t, gn) if npe == 3 else tet_divergence(v, t, gn)
     A, _ = assemble_scipy(v, t, lump=True)
-    I = sparse.eye(A.shape[0])
-    x = poisson(A, I, div)
+    if consistent:
+        x = poisson_neumann_consistent(A, div)
+    else:
+        x = poisson(A, sparse.eye(A.shape[0]), div)
     return x - x.min(axis=0)
 
 
 __all__ = ["tria_local", "tet_local", "assemble_scipy", "assemble_sorted", "csr_sorted_sum", "avg_edge_length",
            "eigs", "eigs_dense", "poisson", "diffusion", "tria_gradient", "tet_gradient", "tria_divergence", "tet_divergence",
-           "normalize_rows", "geodesic_f", "TRIA_IJ", "TET_IJ"]
+           "normalize_rows", "geodesic_f", "poisson_neumann_consistent", "TRIA_IJ", "TET_IJ"]
