@@ -391,8 +391,8 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   const int64_t n = P.n, nnz = P.nnz;
   const int ns = P.nseg, p = P.p, keff = P.keff, lda = P.lda, k = P.k;
   EigPtrs e;
-  e.ct_mem = take(chunk_table_bytes(ns, P.ct.nchunk));
-  e.gt_mem = take(chunk_table_bytes(ns, P.gt.nchunk));
+  e.ct_mem = take(chunk_table_bytes(P.ct));
+  e.gt_mem = take(chunk_table_bytes(P.gt));
   e.diag_pos = (int32_t*)take(4 * n);
   e.k64 = (double*)take(8 * nnz);
   e.k32 = (float*)take(4 * nnz);
@@ -402,7 +402,7 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.Y = (double*)take(8 * n * p);
   e.W = (double*)take(8 * n * p);
   e.MW = (double*)take(8 * n * p);
-  e.ir_bytes = ir_workspace_bytes(n, p, ns, P.ct.nchunk, 1, kPrecJacobi);
+  e.ir_bytes = ir_workspace_bytes(n, p, P.ct, 1, kPrecJacobi);
   e.ir_ws = take(e.ir_bytes);
   const size_t part_elems = (size_t)P.gt.nchunk * std::max((size_t)lda * p, (size_t)keff * keff);
   e.partial = (double*)take(8 * part_elems);

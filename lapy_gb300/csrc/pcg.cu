@@ -1,25 +1,33 @@
 // Persistent cooperative PCG over a block-diagonal batch of CSR systems.
 //
-// One launch runs the whole solve.  Rows are split into chunks that never
-// cross a segment (one mesh = one segment).  Dot products are per (segment, column): each chunk writes its
-// partial sum, and after a grid barrier every CTA that needs a segment's
-// scalar re-reduces that segment's partials in a fixed order, so the result
-// is bitwise reproducible.  Chunks are dealt to CTAs round-robin.  Three barriers per iteration (Jacobi), five with
-// the factored preconditioner z = Gt (G r).  Convergence is tracked per
-// (segment, column); converged columns freeze and fully converged segments
-// skip their rows.  Barriers spin with a bound (common.cuh).
+// One cooperative launch runs the whole solve, warp-centric: the rows are cut
+// into 32-row units (one row per lane), every virtual warp owns a contiguous,
+// row-balanced range of units, and that range is split at segment (mesh)
+// boundaries into pieces.  A piece accumulates its dot-product partials in
+// registers and writes one slot per column; after a grid barrier, any warp
+// that needs a segment's scalar sums that segment's few slots in a fixed
+// order (bitwise reproducible).  Warps never wait for one another except at
+// the grid barriers: three per iteration with the Jacobi preconditioner, five
+// with the factored one z = Gt (G r).  Convergence is tracked per (segment,
+// column): converged columns freeze and converged segments skip their rows.
+// The SpMM stages each unit's contiguous slice of the matrix in the warp's
+// part of shared memory with coalesced loads before the per-row gathers.
+// Barriers spin with a bound (common.cuh).
 #include <climits>
-#include <cstring>
 #include <cmath>
+#include <cstring>
 #include "pcg.cuh"
-#include "spmv.cuh"
 
 namespace lapy {
 
 constexpr int32_t kActive = INT32_MAX;
 constexpr int kPcgThreads = 256;
-// staged nonzeros per tile (values + column indices in shared memory)
-constexpr int kStageCap = 3072;
+constexpr int kWarps = kPcgThreads / 32;
+constexpr int kUnit = 32;
+constexpr int kStageWarp = 384;   // staged nonzeros per warp (values + column indices)
+constexpr int kPlanCtasPerSm = 4; // resident CTAs per SM the warp plan assumes
+
+static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
 int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable* ct) {
   const int64_t total = seg_row[nseg] - seg_row[0];
@@ -31,6 +39,8 @@ int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable*
   ct->h_chunk_row.clear();
   ct->h_chunk_seg.clear();
   ct->h_seg_chunk.assign(nseg + 1, 0);
+  std::vector<int32_t> unit_seg;
+  ct->h_unit_row.clear();
   for (int s = 0; s < nseg; ++s) {
     ct->h_seg_chunk[s] = (int32_t)ct->h_chunk_seg.size();
     const int64_t r0 = seg_row[s], r1 = seg_row[s + 1];
@@ -40,31 +50,73 @@ int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable*
       ct->h_chunk_row.push_back((int32_t)(r0 + len * k / nc));
       ct->h_chunk_seg.push_back(s);
     }
+    for (int64_t r = r0; r < r1; r += kUnit) {
+      ct->h_unit_row.push_back((int32_t)r);
+      unit_seg.push_back(s);
+    }
   }
   ct->h_seg_chunk[nseg] = (int32_t)ct->h_chunk_seg.size();
   ct->h_chunk_row.push_back(seg_row[nseg]);
   ct->nchunk = (int)ct->h_chunk_seg.size();
+  ct->h_unit_row.push_back(seg_row[nseg]);
+  ct->nunit = (int)unit_seg.size();
+
+  // virtual warps: contiguous unit ranges with about total/nvw rows each
+  const int nvw = std::max(1, std::min(ct->nunit, kPlanCtasPerSm * kWarps * lapy_num_sms()));
+  ct->nvw = nvw;
+  std::vector<int32_t> ub(nvw + 1);
+  for (int w = 0; w <= nvw; ++w) {
+    const int64_t target = seg_row[0] + total * w / nvw;
+    ub[w] = (int32_t)(std::lower_bound(ct->h_unit_row.begin(), ct->h_unit_row.begin() + ct->nunit,
+                                       (int32_t)target) - ct->h_unit_row.begin());
+  }
+  ub[nvw] = ct->nunit;
+  ct->h_piece_unit.clear();
+  ct->h_piece_seg.clear();
+  ct->h_vw_piece.assign(nvw + 1, 0);
+  for (int w = 0; w < nvw; ++w) {
+    ct->h_vw_piece[w] = (int32_t)ct->h_piece_seg.size();
+    for (int32_t u = ub[w]; u < ub[w + 1]; ++u) {
+      if (u == ub[w] || unit_seg[u] != unit_seg[u - 1]) {
+        ct->h_piece_unit.push_back(u);
+        ct->h_piece_seg.push_back(unit_seg[u]);
+      }
+    }
+  }
+  ct->npiece = (int)ct->h_piece_seg.size();
+  ct->h_vw_piece[nvw] = ct->npiece;
+  ct->h_piece_unit.push_back(ct->nunit);
+  ct->h_seg_piece.assign(nseg + 1, ct->npiece);
+  for (int p = ct->npiece - 1; p >= 0; --p) ct->h_seg_piece[ct->h_piece_seg[p]] = p;
+  for (int s = nseg - 1; s >= 0; --s)  // segments without rows: empty piece range
+    if (ct->h_seg_piece[s] > ct->h_seg_piece[s + 1]) ct->h_seg_piece[s] = ct->h_seg_piece[s + 1];
   return ct->nchunk;
 }
 
-static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
-
-size_t chunk_table_bytes(int nseg, int nchunk) {
-  return a256(4 * (size_t)(nchunk + 1)) + a256(4 * (size_t)nchunk) + a256(4 * (size_t)(nseg + 1)) +
-         a256(4 * (size_t)(nseg + 1));
+size_t chunk_table_bytes(const ChunkTable& ct) {
+  return a256(4 * (size_t)(ct.nchunk + 1)) + a256(4 * (size_t)ct.nchunk) + a256(4 * (size_t)(ct.nseg + 1)) * 3 +
+         a256(4 * (size_t)(ct.nunit + 1)) + a256(4 * (size_t)(ct.npiece + 1)) + a256(4 * (size_t)ct.npiece) +
+         a256(4 * (size_t)(ct.nvw + 1));
 }
 
 int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream) {
   char* p = (char*)mem;
-  ct->chunk_row = (int32_t*)p; p += a256(4 * (size_t)(ct->nchunk + 1));
-  ct->chunk_seg = (int32_t*)p; p += a256(4 * (size_t)ct->nchunk);
-  ct->seg_chunk = (int32_t*)p; p += a256(4 * (size_t)(ct->nseg + 1));
-  ct->seg_row = (int32_t*)p;
-  LAPY_CUDA_TRY(cudaMemcpyAsync(ct->chunk_row, ct->h_chunk_row.data(), 4 * (ct->nchunk + 1), cudaMemcpyHostToDevice, stream));
-  LAPY_CUDA_TRY(cudaMemcpyAsync(ct->chunk_seg, ct->h_chunk_seg.data(), 4 * ct->nchunk, cudaMemcpyHostToDevice, stream));
-  LAPY_CUDA_TRY(cudaMemcpyAsync(ct->seg_chunk, ct->h_seg_chunk.data(), 4 * (ct->nseg + 1), cudaMemcpyHostToDevice, stream));
-  LAPY_CUDA_TRY(cudaMemcpyAsync(ct->seg_row, ct->h_seg_row.data(), 4 * (ct->nseg + 1), cudaMemcpyHostToDevice, stream));
-  // pageable sources: make sure the copies completed before the vectors change
+  auto put = [&](int32_t** dst, const std::vector<int32_t>& src) -> int {
+    *dst = (int32_t*)p;
+    p += a256(4 * src.size());
+    LAPY_CUDA_TRY(cudaMemcpyAsync(*dst, src.data(), 4 * src.size(), cudaMemcpyHostToDevice, stream));
+    return LAPY_OK;
+  };
+  LAPY_TRY(put(&ct->chunk_row, ct->h_chunk_row));
+  LAPY_TRY(put(&ct->chunk_seg, ct->h_chunk_seg));
+  LAPY_TRY(put(&ct->seg_chunk, ct->h_seg_chunk));
+  LAPY_TRY(put(&ct->seg_row, ct->h_seg_row));
+  LAPY_TRY(put(&ct->unit_row, ct->h_unit_row));
+  LAPY_TRY(put(&ct->piece_unit, ct->h_piece_unit));
+  LAPY_TRY(put(&ct->piece_seg, ct->h_piece_seg));
+  LAPY_TRY(put(&ct->vw_piece, ct->h_vw_piece));
+  LAPY_TRY(put(&ct->seg_piece, ct->h_seg_piece));
+  // pageable sources: the copies must complete before the host vectors change
   LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
   return LAPY_OK;
 }
@@ -76,10 +128,13 @@ struct PcgArgs {
   const int32_t* indices;
   const V* vals;
   PcgPrecondDesc<V> pc;
-  const int32_t* chunk_row;
-  const int32_t* chunk_seg;
-  const int32_t* seg_chunk;
-  int nchunk;
+  const int32_t* unit_row;
+  const int32_t* piece_unit;
+  const int32_t* piece_seg;
+  const int32_t* vw_piece;
+  const int32_t* seg_piece;
+  int nvw;
+  int npiece;
   int nseg;
   const V* B;
   V* X;
@@ -88,7 +143,7 @@ struct PcgArgs {
   V* Q;
   V* Z;
   V* T;
-  double* part;       // [3][nchunk][NP]  pq, rz, rr
+  double* part;       // [3][npiece][NP]  pq, rz, rr
   double* rz;         // [2][nseg][NP]
   double* bb;         // [nseg][NP]
   int32_t* state;     // [2][nseg][NP]
@@ -101,81 +156,6 @@ struct PcgArgs {
   GridBarrier bar;
 };
 
-// Shared scratch of one CTA.
-template <int NP>
-struct PcgShared {
-  double red[kPcgThreads / 32][NP];
-  double s0[NP], s1[NP], s2[NP];
-  double scal[NP];
-  int act[NP];
-  int any;
-  int seg;
-};
-
-// Sum part[c*NP + col] over the chunks of segment s with all threads; thread
-// col < NP receives the column total in out[col].  Fixed order -> deterministic.
-template <int NP>
-__device__ __forceinline__ void seg_reduce(const double* __restrict__ part, int c0, int c1,
-                                           PcgShared<NP>& sh, double* out) {
-  const int t = threadIdx.x;
-  const int col = t % NP;
-  double acc = 0.0;
-  for (int c = c0 + t / NP; c < c1; c += kPcgThreads / NP) acc += part[(int64_t)c * NP + col];
-#pragma unroll
-  for (int o = 16; o >= NP; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  __syncthreads();
-  if ((t & 31) < NP) sh.red[t >> 5][t & 31] = acc;
-  __syncthreads();
-  if (t < NP) {
-    double s = 0.0;
-#pragma unroll
-    for (int w = 0; w < kPcgThreads / 32; ++w) s += sh.red[w][t];
-    out[t] = s;
-  }
-  __syncthreads();
-}
-
-// Reduce a per-thread partial whose column is threadIdx.x % NP over the CTA
-// and store it to part[c*NP + col].
-template <int NP>
-__device__ __forceinline__ void cta_partial_store(double acc, PcgShared<NP>& sh, double* dst) {
-  const int t = threadIdx.x;
-#pragma unroll
-  for (int o = 16; o >= NP; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  __syncthreads();
-  if ((t & 31) < NP) sh.red[t >> 5][t & 31] = acc;
-  __syncthreads();
-  if (t < NP) {
-    double s = 0.0;
-#pragma unroll
-    for (int w = 0; w < kPcgThreads / 32; ++w) s += sh.red[w][t];
-    dst[t] = s;
-  }
-  __syncthreads();
-}
-
-// Reduce per-thread partials of all NP columns (one row per thread) and store
-// them to dst[0..NP).
-template <int NP>
-__device__ __forceinline__ void cta_rows_partial_store(const double (&acc)[NP], PcgShared<NP>& sh,
-                                                       double* dst) {
-  const int t = threadIdx.x;
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < NP; ++q) {
-    const double v = warp_sum(acc[q]);
-    if ((t & 31) == 0) sh.red[t >> 5][q] = v;
-  }
-  __syncthreads();
-  if (t < NP) {
-    double s = 0.0;
-#pragma unroll
-    for (int w = 0; w < kPcgThreads / 32; ++w) s += sh.red[w][t];
-    dst[t] = s;
-  }
-  __syncthreads();
-}
-
 // NP consecutive values of row `row` (vectorised: rows are NP * sizeof(V)
 // aligned because every buffer starts on a 256-byte boundary).
 template <typename V, int NP>
@@ -184,16 +164,16 @@ __device__ __forceinline__ void load_row(const V* __restrict__ base, int64_t row
   if constexpr (sizeof(V) == 4 && NP % 4 == 0) {
 #pragma unroll
     for (int j = 0; j < NP / 4; ++j) {
-      const float4 v = __ldg(reinterpret_cast<const float4*>(p) + j);
+      const float4 v = reinterpret_cast<const float4*>(p)[j];
       out[4 * j] = v.x; out[4 * j + 1] = v.y; out[4 * j + 2] = v.z; out[4 * j + 3] = v.w;
     }
   } else if constexpr (sizeof(V) == 4 && NP == 2) {
-    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    const float2 v = *reinterpret_cast<const float2*>(p);
     out[0] = v.x; out[1] = v.y;
   } else if constexpr (sizeof(V) == 8 && NP % 2 == 0) {
 #pragma unroll
     for (int j = 0; j < NP / 2; ++j) {
-      const double2 v = __ldg(reinterpret_cast<const double2*>(p) + j);
+      const double2 v = reinterpret_cast<const double2*>(p)[j];
       out[2 * j] = v.x; out[2 * j + 1] = v.y;
     }
   } else {
@@ -220,134 +200,169 @@ __device__ __forceinline__ void store_row(V* __restrict__ base, int64_t row, con
   }
 }
 
-// Shared-memory-staged SpMM over the rows [r0, r1) of one chunk: tiles of
-// kPcgThreads rows; the tile's contiguous slice of values and column indices
-// is first copied into shared memory with coalesced loads (every thread keeps
-// several independent loads in flight), then each thread forms one row,
-// gathering the NP-wide rows of Xin.  Tiles longer than the staging buffer
-// read the matrix directly.  With DOT, dacc[q] += Wdot(row, q) * Y(row, q).
+// Sum of a segment's piece slots for every column; afterwards each lane holds
+// all NP totals in tot[] (fixed summation order).
+template <int NP>
+__device__ __forceinline__ void seg_totals(const double* __restrict__ part, int p0, int p1, double (&tot)[NP]) {
+  const int lane = threadIdx.x & 31;
+  constexpr int SPAN = (NP <= 32) ? 32 / NP : 1;
+  double acc = 0.0;
+  for (int p = p0 + lane / NP; p < p1; p += SPAN) acc += part[(int64_t)p * NP + (lane % NP)];
+#pragma unroll
+  for (int o = 16; o >= NP; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+#pragma unroll
+  for (int q = 0; q < NP; ++q) tot[q] = __shfl_sync(0xffffffffu, acc, q);
+}
+
+// Warp-reduce per-lane column partials and store them to dst[0..NP).
+template <int NP>
+__device__ __forceinline__ void warp_store_partials(const float (&acc)[NP], double* dst) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    const double v = warp_sum((double)acc[q]);
+    if (lane == q) dst[q] = v;
+  }
+}
+
+// Y = Mat * Xin on the 32 rows [ur0, ur1) of one unit (lane = row): the unit's
+// contiguous slice of values and column indices is staged in the warp's part
+// of shared memory with coalesced loads, then each lane gathers the NP-wide
+// rows of Xin.  Slices longer than the staging space read the matrix directly.
+// With DOT, dacc[q] += Wdot(row, q) * Y(row, q).
 template <typename V, int NP, bool DOT>
-__device__ __forceinline__ void chunk_spmm(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                                           const V* __restrict__ val, const V* __restrict__ Xin,
-                                           V* __restrict__ Y, const V* __restrict__ Wdot, int r0, int r1,
-                                           V* __restrict__ sval, int32_t* __restrict__ sidx,
-                                           double (&dacc)[NP]) {
-  const int t = threadIdx.x;
-  for (int tr0 = r0; tr0 < r1; tr0 += kPcgThreads) {
-    const int tr1 = min(tr0 + kPcgThreads, r1);
-    const int32_t k0 = ptr[tr0], k1 = ptr[tr1];
-    const bool staged = (k1 - k0) <= kStageCap;
-    __syncthreads();  // the previous tile is done with the staging buffer
-    if (staged) {
-      for (int32_t e = t; e < k1 - k0; e += kPcgThreads) {
-        sval[e] = val[k0 + e];
-        sidx[e] = idx[k0 + e];
-      }
+__device__ __forceinline__ void unit_spmm(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                          const V* __restrict__ val, const V* __restrict__ Xin,
+                                          V* __restrict__ Y, const V* __restrict__ Wdot, int ur0, int ur1,
+                                          V* __restrict__ wval, int32_t* __restrict__ widx, float (&dacc)[NP]) {
+  const int lane = threadIdx.x & 31;
+  const int32_t k0 = ptr[ur0], k1 = ptr[ur1];
+  const bool staged = (k1 - k0) <= kStageWarp;
+  __syncwarp();  // the previous unit's slice is no longer read
+  if (staged) {
+    for (int32_t e = lane; e < k1 - k0; e += 32) {
+      wval[e] = val[k0 + e];
+      widx[e] = idx[k0 + e];
     }
-    __syncthreads();
-    const int row = tr0 + t;
-    if (row < tr1) {
-      const int32_t kb = ptr[row], ke = ptr[row + 1];
-      V acc[NP];
+  }
+  __syncwarp();
+  const int row = ur0 + lane;
+  if (row < ur1) {
+    const int32_t kb = ptr[row], ke = ptr[row + 1];
+    V acc[NP];
 #pragma unroll
-      for (int q = 0; q < NP; ++q) acc[q] = V(0);
+    for (int q = 0; q < NP; ++q) acc[q] = V(0);
 #pragma unroll 4
-      for (int32_t k = kb; k < ke; ++k) {
-        const V a = staged ? sval[k - k0] : val[k];
-        const int32_t c = staged ? sidx[k - k0] : idx[k];
-        V xr[NP];
-        load_row<V, NP>(Xin, c, xr);
+    for (int32_t k = kb; k < ke; ++k) {
+      const V a = staged ? wval[k - k0] : val[k];
+      const int32_t c = staged ? widx[k - k0] : idx[k];
+      V xr[NP];
+      load_row<V, NP>(Xin, c, xr);
 #pragma unroll
-        for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
-      }
-      store_row<V, NP>(Y, row, acc);
-      if (DOT) {
-        V w[NP];
-        load_row<V, NP>(Wdot, row, w);
+      for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
+    }
+    store_row<V, NP>(Y, row, acc);
+    if (DOT) {
+      V w[NP];
+      load_row<V, NP>(Wdot, row, w);
 #pragma unroll
-        for (int q = 0; q < NP; ++q) dacc[q] += (double)(w[q] * acc[q]);
-      }
+      for (int q = 0; q < NP; ++q) dacc[q] += (float)(w[q] * acc[q]);
     }
   }
 }
 
+// Loop over this warp's pieces: s = segment, [u0, u1) = units of the piece.
+#define FOR_MY_PIECES(a, ...)                                                               \
+  for (int vw = gw; vw < (a).nvw; vw += nw) {                                                \
+    for (int p = (a).vw_piece[vw]; p < (a).vw_piece[vw + 1]; ++p) {                          \
+      const int s = (a).piece_seg[p];                                                        \
+      const int u0 = (a).piece_unit[p], u1 = (a).piece_unit[p + 1];                          \
+      (void)s; (void)u0; (void)u1;                                                           \
+      __VA_ARGS__                                                                            \
+    }                                                                                        \
+  }
+
 template <typename V, int NP, int PC>
 __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
-  __shared__ PcgShared<NP> sh;
-  extern __shared__ __align__(16) unsigned char stage_raw[];
-  V* sval = reinterpret_cast<V*>(stage_raw);
-  int32_t* sidx = reinterpret_cast<int32_t*>(stage_raw + sizeof(V) * kStageCap);
-  const int t = threadIdx.x;
-  // Chunks are dealt round-robin: every CTA holds pieces of many segments,
-  // so the work stays balanced while segments converge at different times.
-  const int c_begin = blockIdx.x, c_step = gridDim.x;
-  const int c_end = a.nchunk;
+  __shared__ V sval_all[kWarps * kStageWarp];
+  __shared__ int32_t sidx_all[kWarps * kStageWarp];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gw = blockIdx.x * kWarps + warp, nw = gridDim.x * kWarps;
+  V* wval = sval_all + warp * kStageWarp;
+  int32_t* widx = sidx_all + warp * kStageWarp;
   double* part_pq = a.part;
-  double* part_rz = a.part + (int64_t)a.nchunk * NP;
-  double* part_rr = a.part + 2 * (int64_t)a.nchunk * NP;
-  const int colt = t % NP;  // fixed column of this thread in element-wise loops
-  constexpr int U = 4;      // element-wise unroll: U independent streams per thread
+  double* part_rz = a.part + (int64_t)a.npiece * NP;
+  double* part_rr = a.part + 2 * (int64_t)a.npiece * NP;
 
-  // ---- phase 0: X = 0, R = B, Z = M^-1 R, P = Z; partial b'b and r'z
-  for (int c = c_begin; c < c_end; c += c_step) {
-    const int64_t e0 = (int64_t)a.chunk_row[c] * NP, e1 = (int64_t)a.chunk_row[c + 1] * NP;
-    double bb = 0.0, rz = 0.0;
-    for (int64_t i = e0 + t; i < e1; i += kPcgThreads) {
-      const V b = a.B[i];
-      a.X[i] = V(0);
-      a.R[i] = b;
-      bb += (double)b * (double)b;
-      if (PC == kPrecJacobi) {
-        const V z = a.pc.dinv[i / NP] * b;
-        a.P[i] = z;
-        rz += (double)b * (double)z;
+  // ---- phase 0: X = 0, R = B, P = M^-1 R (Jacobi); partial b'b and r'z
+  FOR_MY_PIECES(a, {
+    float bb[NP], rz[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) { bb[q] = 0.f; rz[q] = 0.f; }
+    for (int u = u0; u < u1; ++u) {
+      const int row = a.unit_row[u] + lane;
+      if (row < a.unit_row[u + 1]) {
+        V b[NP], z[NP], zero[NP];
+        load_row<V, NP>(a.B, row, b);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) zero[q] = V(0);
+        store_row<V, NP>(a.X, row, zero);
+        store_row<V, NP>(a.R, row, b);
+        if (PC == kPrecJacobi) {
+          const V d = a.pc.dinv[row];
+#pragma unroll
+          for (int q = 0; q < NP; ++q) { z[q] = d * b[q]; rz[q] += (float)(b[q] * z[q]); }
+          store_row<V, NP>(a.P, row, z);
+        }
+#pragma unroll
+        for (int q = 0; q < NP; ++q) bb[q] += (float)(b[q] * b[q]);
       }
     }
-    cta_partial_store<NP>(bb, sh, part_rr + (int64_t)c * NP);
-    if (PC == kPrecJacobi) cta_partial_store<NP>(rz, sh, part_rz + (int64_t)c * NP);
-  }
+    warp_store_partials<NP>(bb, part_rr + (int64_t)p * NP);
+    if (PC == kPrecJacobi) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
+  })
   if (PC == kPrecFactored) {
+    float dummy[NP];
     if (!grid_sync(a.bar)) return;
-    double dummy[NP];
-    for (int c = c_begin; c < c_end; c += c_step)
-      chunk_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.chunk_row[c],
-                               a.chunk_row[c + 1], sval, sidx, dummy);
+    FOR_MY_PIECES(a, {
+      for (int u = u0; u < u1; ++u)
+        unit_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.unit_row[u],
+                                a.unit_row[u + 1], wval, widx, dummy);
+    })
     if (!grid_sync(a.bar)) return;
-    for (int c = c_begin; c < c_end; c += c_step) {
-      double acc[NP];
+    FOR_MY_PIECES(a, {
+      float acc[NP];
 #pragma unroll
-      for (int j = 0; j < NP; ++j) acc[j] = 0.0;
-      chunk_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R, a.chunk_row[c],
-                              a.chunk_row[c + 1], sval, sidx, acc);
-      cta_rows_partial_store<NP>(acc, sh, part_rz + (int64_t)c * NP);
-    }
-    if (!grid_sync(a.bar)) return;
-    for (int c = c_begin; c < c_end; c += c_step) {
-      const int64_t e0 = (int64_t)a.chunk_row[c] * NP, e1 = (int64_t)a.chunk_row[c + 1] * NP;
-      for (int64_t i = e0 + t; i < e1; i += kPcgThreads) a.P[i] = a.Z[i];
-    }
+      for (int q = 0; q < NP; ++q) acc[q] = 0.f;
+      for (int u = u0; u < u1; ++u)
+        unit_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.P, a.R, a.unit_row[u],
+                               a.unit_row[u + 1], wval, widx, acc);
+      warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
+    })
   }
   if (!grid_sync(a.bar)) return;
-  // ---- segment initialisation (first chunk of each segment publishes)
-  for (int c = c_begin; c < c_end; c += c_step) {
-    const int s = a.chunk_seg[c];
-    if (a.seg_chunk[s] != c) continue;
-    seg_reduce<NP>(part_rr, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s0);
-    seg_reduce<NP>(part_rz, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s1);
-    if (t < NP) {
-      const double bb = sh.s0[t], rz = sh.s1[t];
-      int32_t st;
-      if (!isfinite(bb) || !isfinite(rz)) st = LAPY_ERR_NAN;
-      else if (bb == 0.0) st = 0;
-      else if (!(rz > 0.0)) st = LAPY_ERR_BREAKDOWN;
-      else st = kActive;
-      a.bb[s * NP + t] = bb;
-      a.rz[s * NP + t] = rz;
-      a.state[s * NP + t] = st;
-      if (st == kActive) atomicAdd(&a.active[0], 1u);
+  // ---- segment initialisation (the warp holding a segment's first piece publishes)
+  FOR_MY_PIECES(a, {
+    if (a.seg_piece[s] == p) {
+      double bb[NP], rz[NP];
+      seg_totals<NP>(part_rr, a.seg_piece[s], a.seg_piece[s + 1], bb);
+      seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rz);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        if (lane == q) {
+          int32_t st;
+          if (!isfinite(bb[q]) || !isfinite(rz[q])) st = LAPY_ERR_NAN;
+          else if (bb[q] == 0.0) st = 0;
+          else if (!(rz[q] > 0.0)) st = LAPY_ERR_BREAKDOWN;
+          else st = kActive;
+          a.bb[s * NP + q] = bb[q];
+          a.rz[s * NP + q] = rz[q];
+          a.state[s * NP + q] = st;
+          if (st == kActive) atomicAdd(&a.active[0], 1u);
+        }
+      }
     }
-    __syncthreads();
-  }
+  })
   if (!grid_sync(a.bar)) return;
 
   int it = 0;
@@ -361,206 +376,166 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
     if (nact == 0 || it >= a.maxiter) break;
 
     // ---- phase A: Q = K P, partial p'q
-    if (blockIdx.x == 0 && t == 0) a.active[par ^ 1] = 0u;
-    if (t == 0) sh.seg = -1;
-    __syncthreads();
-    for (int c = c_begin; c < c_end; c += c_step) {
-      const int s = a.chunk_seg[c];
-      if (s != sh.seg) {
-        __syncthreads();
-        if (t == 0) {
-          int any = 0;
-          for (int q = 0; q < NP; ++q) any |= (st_cur[s * NP + q] == kActive);
-          sh.any = any;
-          sh.seg = s;
-        }
-        __syncthreads();
-      }
-      if (!sh.any) {
-        if (t < NP) part_pq[(int64_t)c * NP + t] = 0.0;
-        continue;
-      }
-      double acc[NP];
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.active[par ^ 1] = 0u;
+    FOR_MY_PIECES(a, {
+      const bool any = __any_sync(0xffffffffu, lane < NP && st_cur[s * NP + (lane % NP)] == kActive);
+      float acc[NP];
 #pragma unroll
-      for (int j = 0; j < NP; ++j) acc[j] = 0.0;
-      chunk_spmm<V, NP, true>(a.indptr, a.indices, a.vals, a.P, a.Q, a.P, a.chunk_row[c], a.chunk_row[c + 1],
-                              sval, sidx, acc);
-      cta_rows_partial_store<NP>(acc, sh, part_pq + (int64_t)c * NP);
-      if (t == 0) {
-        const int r0 = a.chunk_row[c], r1 = a.chunk_row[c + 1];
-        atomicAdd(&a.work[0], (unsigned long long)(r1 - r0));
-        atomicAdd(&a.work[1], (unsigned long long)(a.indptr[r1] - a.indptr[r0]));
+      for (int q = 0; q < NP; ++q) acc[q] = 0.f;
+      if (any) {
+        for (int u = u0; u < u1; ++u)
+          unit_spmm<V, NP, true>(a.indptr, a.indices, a.vals, a.P, a.Q, a.P, a.unit_row[u], a.unit_row[u + 1],
+                                 wval, widx, acc);
+        if (lane == 0) {
+          const int r0 = a.unit_row[u0], r1 = a.unit_row[u1];
+          atomicAdd(&a.work[0], (unsigned long long)(r1 - r0));
+          atomicAdd(&a.work[1], (unsigned long long)(a.indptr[r1] - a.indptr[r0]));
+        }
       }
-    }
+      warp_store_partials<NP>(acc, part_pq + (int64_t)p * NP);
+    })
     if (!grid_sync(a.bar)) return;
 
     // ---- phase B: alpha, X += alpha P, R -= alpha Q, partial r'r (and r'z for Jacobi)
-    if (t == 0) sh.seg = -1;
-    __syncthreads();
-    for (int c = c_begin; c < c_end; c += c_step) {
-      const int s = a.chunk_seg[c];
-      if (s != sh.seg) {
-        seg_reduce<NP>(part_pq, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s0);
-        if (t < NP) {
-          const double pq = sh.s0[t];
-          const bool act = st_cur[s * NP + t] == kActive;
-          const bool ok = act && pq > 0.0 && isfinite(pq);
-          sh.scal[t] = ok ? rz_cur[s * NP + t] / pq : 0.0;
-          sh.act[t] = ok;
-        }
-        if (t == 0) sh.seg = s;
-        __syncthreads();
-        if (t == 0) {
-          int any = 0;
-          for (int q = 0; q < NP; ++q) any |= sh.act[q];
-          sh.any = any;
-        }
-        __syncthreads();
-      }
-      const int64_t e0 = (int64_t)a.chunk_row[c] * NP, e1 = (int64_t)a.chunk_row[c + 1] * NP;
-      if (!sh.any) {
-        if (t < NP) {
-          part_rr[(int64_t)c * NP + t] = 0.0;
-          part_rz[(int64_t)c * NP + t] = 0.0;
-        }
-        continue;
-      }
-      const V alpha = (V)sh.scal[colt];
-      const bool act = sh.act[colt];
-      float rr = 0.f, rz = 0.f;
-      for (int64_t i0 = e0 + t; i0 < e1; i0 += U * kPcgThreads) {
-        V xv[U], pv[U], qv[U], rv[U], dv[U];
+    FOR_MY_PIECES(a, {
+      double pq[NP];
+      seg_totals<NP>(part_pq, a.seg_piece[s], a.seg_piece[s + 1], pq);
+      V alpha[NP];
+      bool act[NP];
+      bool any = false;
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int64_t i = i0 + u * kPcgThreads;
-          if (i < e1) {
-            rv[u] = a.R[i];
-            if (act) { xv[u] = a.X[i]; pv[u] = a.P[i]; qv[u] = a.Q[i]; }
-            if (PC == kPrecJacobi) dv[u] = a.pc.dinv[i / NP];
-          }
-        }
+      for (int q = 0; q < NP; ++q) {
+        act[q] = st_cur[s * NP + q] == kActive && pq[q] > 0.0 && isfinite(pq[q]);
+        alpha[q] = act[q] ? (V)(rz_cur[s * NP + q] / pq[q]) : V(0);
+        any |= act[q];
+      }
+      float rr[NP], rz[NP];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int64_t i = i0 + u * kPcgThreads;
-          if (i < e1) {
-            V r = rv[u];
-            if (act) {
-              a.X[i] = xv[u] + alpha * pv[u];
-              r = r - alpha * qv[u];
-              a.R[i] = r;
+      for (int q = 0; q < NP; ++q) { rr[q] = 0.f; rz[q] = 0.f; }
+      if (any) {
+        for (int u = u0; u < u1; ++u) {
+          const int row = a.unit_row[u] + lane;
+          if (row < a.unit_row[u + 1]) {
+            V x[NP], pv[NP], qv[NP], r[NP];
+            load_row<V, NP>(a.X, row, x);
+            load_row<V, NP>(a.P, row, pv);
+            load_row<V, NP>(a.Q, row, qv);
+            load_row<V, NP>(a.R, row, r);
+            const V d = (PC == kPrecJacobi) ? a.pc.dinv[row] : V(0);
+#pragma unroll
+            for (int q = 0; q < NP; ++q) {
+              if (act[q]) {
+                x[q] = x[q] + alpha[q] * pv[q];
+                r[q] = r[q] - alpha[q] * qv[q];
+              }
+              rr[q] += (float)(r[q] * r[q]);
+              if (PC == kPrecJacobi) rz[q] += (float)(r[q] * (d * r[q]));
             }
-            rr += (float)(r * r);
-            if (PC == kPrecJacobi) rz += (float)(r * (dv[u] * r));
+            store_row<V, NP>(a.X, row, x);
+            store_row<V, NP>(a.R, row, r);
           }
         }
       }
-      cta_partial_store<NP>((double)rr, sh, part_rr + (int64_t)c * NP);
-      if (PC == kPrecJacobi) cta_partial_store<NP>((double)rz, sh, part_rz + (int64_t)c * NP);
-    }
+      warp_store_partials<NP>(rr, part_rr + (int64_t)p * NP);
+      if (PC == kPrecJacobi) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
+    })
     if (!grid_sync(a.bar)) return;
 
     if (PC == kPrecFactored) {
       // ---- phase B2: T = G R ; phase B3: Z = Gt T, partial r'z
-      double dummy[NP];
-      for (int c = c_begin; c < c_end; c += c_step)
-        chunk_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.chunk_row[c],
-                                 a.chunk_row[c + 1], sval, sidx, dummy);
+      float dummy[NP];
+      FOR_MY_PIECES(a, {
+        for (int u = u0; u < u1; ++u)
+          unit_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.unit_row[u],
+                                  a.unit_row[u + 1], wval, widx, dummy);
+      })
       if (!grid_sync(a.bar)) return;
-      for (int c = c_begin; c < c_end; c += c_step) {
-        double acc[NP];
+      FOR_MY_PIECES(a, {
+        float acc[NP];
 #pragma unroll
-        for (int j = 0; j < NP; ++j) acc[j] = 0.0;
-        chunk_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R, a.chunk_row[c],
-                                a.chunk_row[c + 1], sval, sidx, acc);
-        cta_rows_partial_store<NP>(acc, sh, part_rz + (int64_t)c * NP);
-      }
+        for (int q = 0; q < NP; ++q) acc[q] = 0.f;
+        for (int u = u0; u < u1; ++u)
+          unit_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R, a.unit_row[u],
+                                 a.unit_row[u + 1], wval, widx, acc);
+        warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
+      })
       if (!grid_sync(a.bar)) return;
     }
 
     // ---- phase C: convergence, beta, P = Z + beta P
-    if (t == 0) sh.seg = -1;
-    __syncthreads();
-    for (int c = c_begin; c < c_end; c += c_step) {
-      const int s = a.chunk_seg[c];
-      if (s != sh.seg) {
-        seg_reduce<NP>(part_pq, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s0);
-        seg_reduce<NP>(part_rz, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s1);
-        seg_reduce<NP>(part_rr, a.seg_chunk[s], a.seg_chunk[s + 1], sh, sh.s2);
-        if (t < NP) {
-          const int32_t st0 = st_cur[s * NP + t];
-          const double pq = sh.s0[t], rzn = sh.s1[t], rr = sh.s2[t];
-          int32_t st = st0;
-          if (st0 == kActive) {
-            if (!(pq > 0.0) || !isfinite(pq)) st = LAPY_ERR_BREAKDOWN;
-            else if (!isfinite(rr) || !isfinite(rzn)) st = LAPY_ERR_NAN;
-            else if (rr <= a.rtol2 * a.bb[s * NP + t]) st = it + 1;
-            else if (!(rzn > 0.0)) st = LAPY_ERR_BREAKDOWN;
-          }
-          const bool act = st == kActive;
-          sh.scal[t] = act ? rzn / rz_cur[s * NP + t] : 0.0;
-          sh.act[t] = act;
-          if (a.seg_chunk[s] == c) {  // a segment's first chunk always starts a new run
-            st_nxt[s * NP + t] = st;
-            rz_nxt[s * NP + t] = rzn;
-            if (act) atomicAdd(&a.active[par ^ 1], 1u);
-          }
-        }
-        if (t == 0) sh.seg = s;
-        __syncthreads();
-        if (t == 0) {
-          int any = 0;
-          for (int q = 0; q < NP; ++q) any |= sh.act[q];
-          sh.any = any;
-        }
-        __syncthreads();
-      }
-      if (!sh.any) continue;
-      const int64_t e0 = (int64_t)a.chunk_row[c] * NP, e1 = (int64_t)a.chunk_row[c + 1] * NP;
-      const V beta = (V)sh.scal[colt];
-      if (sh.act[colt]) {
-        for (int64_t i0 = e0 + t; i0 < e1; i0 += U * kPcgThreads) {
-          V zv[U], pv[U];
+    FOR_MY_PIECES(a, {
+      double pq[NP], rzn[NP], rr[NP];
+      seg_totals<NP>(part_pq, a.seg_piece[s], a.seg_piece[s + 1], pq);
+      seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rzn);
+      seg_totals<NP>(part_rr, a.seg_piece[s], a.seg_piece[s + 1], rr);
+      V beta[NP];
+      bool act[NP];
+      bool any = false;
+      const bool first = a.seg_piece[s] == p;
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            const int64_t i = i0 + u * kPcgThreads;
-            if (i < e1) {
-              zv[u] = (PC == kPrecJacobi) ? a.pc.dinv[i / NP] * a.R[i] : a.Z[i];
-              pv[u] = a.P[i];
+      for (int q = 0; q < NP; ++q) {
+        const int32_t st0 = st_cur[s * NP + q];
+        int32_t st = st0;
+        if (st0 == kActive) {
+          if (!(pq[q] > 0.0) || !isfinite(pq[q])) st = LAPY_ERR_BREAKDOWN;
+          else if (!isfinite(rr[q]) || !isfinite(rzn[q])) st = LAPY_ERR_NAN;
+          else if (rr[q] <= a.rtol2 * a.bb[s * NP + q]) st = it + 1;
+          else if (!(rzn[q] > 0.0)) st = LAPY_ERR_BREAKDOWN;
+        }
+        act[q] = st == kActive;
+        beta[q] = act[q] ? (V)(rzn[q] / rz_cur[s * NP + q]) : V(0);
+        any |= act[q];
+        if (first && lane == q) {
+          st_nxt[s * NP + q] = st;
+          rz_nxt[s * NP + q] = rzn[q];
+          if (act[q]) atomicAdd(&a.active[par ^ 1], 1u);
+        }
+      }
+      if (any) {
+        for (int u = u0; u < u1; ++u) {
+          const int row = a.unit_row[u] + lane;
+          if (row < a.unit_row[u + 1]) {
+            V z[NP], pv[NP];
+            if (PC == kPrecJacobi) {
+              const V d = a.pc.dinv[row];
+              load_row<V, NP>(a.R, row, z);
+#pragma unroll
+              for (int q = 0; q < NP; ++q) z[q] = d * z[q];
+            } else {
+              load_row<V, NP>(a.Z, row, z);
             }
-          }
+            load_row<V, NP>(a.P, row, pv);
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            const int64_t i = i0 + u * kPcgThreads;
-            if (i < e1) a.P[i] = zv[u] + beta * pv[u];
+            for (int q = 0; q < NP; ++q)
+              if (act[q]) pv[q] = z[q] + beta[q] * pv[q];
+            store_row<V, NP>(a.P, row, pv);
           }
         }
       }
-    }
+    })
     if (!grid_sync(a.bar)) return;
   }
 
-  // ---- publish the final state (first chunk of each segment)
+  // ---- publish the final state (the warp holding a segment's first piece)
   const int par = it & 1;
-  const int32_t* st_cur = a.state + par * (int64_t)a.nseg * NP;
-  for (int c = c_begin; c < c_end; c += c_step) {
-    const int s = a.chunk_seg[c];
-    if (a.seg_chunk[s] != c) continue;
-    if (t < NP) {
-      int32_t st = st_cur[s * NP + t];
+  const int32_t* st_fin = a.state + par * (int64_t)a.nseg * NP;
+  FOR_MY_PIECES(a, {
+    if (a.seg_piece[s] == p && lane < NP) {
+      int32_t st = st_fin[s * NP + lane];
       if (st == kActive) st = LAPY_ERR_NOCONV;
-      a.state_out[s * NP + t] = st;
+      a.state_out[s * NP + lane] = st;
     }
-  }
-  if (blockIdx.x == 0 && t == 0) a.iters[0] = it;
+  })
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.iters[0] = it;
 }
 
-size_t pcg_workspace_bytes(int64_t n, int p, int nseg, int nchunk, int elem_size, int precond) {
+size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond) {
   const size_t vec = a256((size_t)n * p * elem_size);
   size_t b = vec * (precond == kPrecFactored ? 5 : 3);  // R P Q (+ Z T)
-  b += a256(sizeof(double) * 3 * (size_t)nchunk * p);
-  b += a256(sizeof(double) * 2 * (size_t)nseg * p);
-  b += a256(sizeof(double) * (size_t)nseg * p);
-  b += a256(sizeof(int32_t) * 2 * (size_t)nseg * p);
+  b += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
+  b += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
+  b += a256(sizeof(double) * (size_t)ct.nseg * p);
+  b += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
   b += a256(64);  // active[2], iters, barrier, work counters
   return b + 256;
 }
@@ -568,16 +543,16 @@ size_t pcg_workspace_bytes(int64_t n, int p, int nseg, int nchunk, int elem_size
 template <typename V, int NP, int PC>
 static int launch_pcg(PcgArgs<V>& args, cudaStream_t stream) {
   auto kern = pcg_kernel<V, NP, PC>;
-  const size_t smem = (sizeof(V) + sizeof(int32_t)) * kStageCap;
   int per_sm = 0;
-  LAPY_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPcgThreads, smem));
+  LAPY_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPcgThreads, 0));
   if (per_sm <= 0) {
     lapy_set_last_message("pcg: kernel cannot be resident (occupancy 0)");
     return LAPY_ERR_CUDA;
   }
-  const int grid = std::max(1, std::min(per_sm * lapy_num_sms(), args.nchunk));
+  per_sm = std::min(per_sm, kPlanCtasPerSm);
+  const int grid = std::max(1, std::min(per_sm * lapy_num_sms(), (args.nvw + kWarps - 1) / kWarps));
   void* kargs[] = {(void*)&args};
-  LAPY_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kPcgThreads), kargs, smem, stream));
+  LAPY_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kPcgThreads), kargs, 0, stream));
   return lapy_check_launch("pcg_kernel");
 }
 
@@ -600,8 +575,7 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
               const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct, const V* B, V* X,
               double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
               cudaStream_t stream, int* iters_out) {
-  if (ws_bytes < pcg_workspace_bytes(n, p, ct.nseg, ct.nchunk, sizeof(V), pc.kind))
-    return LAPY_ERR_WORKSPACE;
+  if (ws_bytes < pcg_workspace_bytes(n, p, ct, sizeof(V), pc.kind)) return LAPY_ERR_WORKSPACE;
   char* w = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
   const size_t vec = a256((size_t)n * p * sizeof(V));
   PcgArgs<V> a;
@@ -610,10 +584,13 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
   a.indices = indices;
   a.vals = vals;
   a.pc = pc;
-  a.chunk_row = ct.chunk_row;
-  a.chunk_seg = ct.chunk_seg;
-  a.seg_chunk = ct.seg_chunk;
-  a.nchunk = ct.nchunk;
+  a.unit_row = ct.unit_row;
+  a.piece_unit = ct.piece_unit;
+  a.piece_seg = ct.piece_seg;
+  a.vw_piece = ct.vw_piece;
+  a.seg_piece = ct.seg_piece;
+  a.nvw = ct.nvw;
+  a.npiece = ct.npiece;
   a.nseg = ct.nseg;
   a.B = B;
   a.X = X;
@@ -626,11 +603,11 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
     a.Z = (V*)w; w += vec;
     a.T = (V*)w; w += vec;
   }
-  a.part = (double*)w; w += a256(sizeof(double) * 3 * (size_t)ct.nchunk * p);
+  a.part = (double*)w; w += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
   a.rz = (double*)w; w += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
   a.bb = (double*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
   a.state = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
-  unsigned* ctl = (unsigned*)w;  // active[2], iters, count, gen, err
+  unsigned* ctl = (unsigned*)w;  // active[2], iters, count, gen, err, work[2] (u64)
   a.active = ctl;
   a.iters = (int*)(ctl + 2);
   a.bar.count = ctl + 3;
@@ -641,6 +618,8 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
   a.rtol2 = rtol * rtol;
   a.maxiter = maxiter;
   LAPY_CUDA_TRY(cudaMemsetAsync(ctl, 0, 64, stream));
+  // segments without rows have no piece: they are reported as solved
+  LAPY_CUDA_TRY(cudaMemsetAsync(state_dev, 0, sizeof(int32_t) * (size_t)ct.nseg * p, stream));
   int st;
   const bool prof = lapy_profile_enabled();
   cudaEvent_t e0 = nullptr, e1 = nullptr;

@@ -5,8 +5,16 @@
 
 namespace lapy {
 
-// Rows are grouped into chunks that never cross a segment (mesh) boundary.
-// A persistent CTA owns a contiguous range of chunks.
+// Work decomposition of a block-diagonal batch (one segment = one mesh).
+//
+// chunks  rows grouped into pieces that never cross a segment (used by the
+//         segmented GEMM / norm kernels, one CTA per chunk)
+// units   32-row blocks inside a segment (one row per lane of a warp)
+// vwarps  "virtual warps" of the persistent PCG: each owns a contiguous,
+//         row-balanced range of units
+// pieces  a virtual warp's unit range cut at segment boundaries; every piece
+//         owns one partial-sum slot, so a segment's dot products are the sum
+//         of its (few) pieces' partials, in a fixed order
 struct ChunkTable {
   int nseg = 0;
   int nchunk = 0;
@@ -14,15 +22,23 @@ struct ChunkTable {
   int32_t* chunk_seg = nullptr;  // device, nchunk
   int32_t* seg_chunk = nullptr;  // device, nseg + 1
   int32_t* seg_row = nullptr;    // device, nseg + 1
+  int nunit = 0, npiece = 0, nvw = 0;
+  int32_t* unit_row = nullptr;    // device, nunit + 1
+  int32_t* piece_unit = nullptr;  // device, npiece + 1
+  int32_t* piece_seg = nullptr;   // device, npiece
+  int32_t* vw_piece = nullptr;    // device, nvw + 1
+  int32_t* seg_piece = nullptr;   // device, nseg + 1
   std::vector<int32_t> h_seg_row;
   std::vector<int32_t> h_chunk_row, h_chunk_seg, h_seg_chunk;
+  std::vector<int32_t> h_unit_row, h_piece_unit, h_piece_seg, h_vw_piece, h_seg_piece;
 };
 
-// Plan chunks for the given segments (host); returns the chunk count.
-int plan_chunks(const int32_t* seg_row_host, int nseg, int target_chunks, ChunkTable* ct);
-// Bytes of device memory the chunk table needs.
-size_t chunk_table_bytes(int nseg, int nchunk);
-// Place the table into `mem` and upload it (async on `stream`).
+// Plan chunks (and the PCG's warp plan) for the given segments (host);
+// returns the chunk count.
+int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable* ct);
+// Bytes of device memory the table needs.
+size_t chunk_table_bytes(const ChunkTable& ct);
+// Place the table into `mem` and upload it (synchronous on `stream`).
 int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream);
 
 enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1 };
@@ -42,7 +58,7 @@ struct PcgPrecondDesc {
 };
 
 // Scratch needed by one persistent PCG solve of n rows x p columns.
-size_t pcg_workspace_bytes(int64_t n, int p, int nseg, int nchunk, int elem_size, int precond);
+size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond);
 
 // Per-(segment, column) outcome codes written to `state`:
 //   > 0  converged after that many iterations (1-based)

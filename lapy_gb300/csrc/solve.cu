@@ -9,14 +9,15 @@ namespace lapy {
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-size_t ir_workspace_bytes(int64_t n, int p, int nseg, int nchunk, int mixed, int precond) {
+size_t ir_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int mixed, int precond) {
+  const int nseg = ct.nseg;
   size_t b = 0;
   b += a256(sizeof(double) * n * p);            // R64
   b += a256(sizeof(float) * n * p) * 2;         // R32, D32
   b += a256(sizeof(double) * nseg * p) * 2;     // bn2, rn2
   b += a256(sizeof(int32_t) * nseg * p) * 2;    // state, mask
-  b += mixed ? pcg_workspace_bytes(n, p, nseg, nchunk, sizeof(float), precond)
-             : pcg_workspace_bytes(n, p, nseg, nchunk, sizeof(double), kPrecJacobi);
+  b += mixed ? pcg_workspace_bytes(n, p, ct, sizeof(float), precond)
+             : pcg_workspace_bytes(n, p, ct, sizeof(double), kPrecJacobi);
   return b + 512;
 }
 
@@ -38,7 +39,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
   const int64_t n = K.n;
   const int nsp = ct.nseg * p;
   const int precond = mixed ? K.pc32.kind : kPrecJacobi;
-  if (ws_bytes < ir_workspace_bytes(n, p, ct.nseg, ct.nchunk, mixed, precond)) return LAPY_ERR_WORKSPACE;
+  if (ws_bytes < ir_workspace_bytes(n, p, ct, mixed, precond)) return LAPY_ERR_WORKSPACE;
   char* w = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
   double* R64 = (double*)w; w += a256(sizeof(double) * n * p);
   float* R32 = (float*)w; w += a256(sizeof(float) * n * p);
@@ -225,8 +226,8 @@ static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed
   char* p3 = take(sizeof(float) * nnz);
   char* p4 = take(sizeof(double) * n * p);
   char* p5 = take(sizeof(double) * n * p);
-  char* p6 = take(chunk_table_bytes(nseg, ct.nchunk));
-  const size_t irb = ir_workspace_bytes(n, p, nseg, ct.nchunk, mixed, kPrecJacobi);
+  char* p6 = take(chunk_table_bytes(ct));
+  const size_t irb = ir_workspace_bytes(n, p, ct, mixed, kPrecJacobi);
   char* p7 = take(irb);
   if (base) {
     *diag_pos = (int32_t*)p0;

@@ -23,12 +23,11 @@ struct IrStats {
   int status = LAPY_OK;
 };
 
-size_t ir_workspace_bytes(int64_t n, int p, int nseg, int nchunk, int mixed, int precond);
+size_t ir_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int mixed, int precond);
 
 // Solve K X = B for p columns (p in {1,2,4,8,16}); X overwritten.  On return
 // relres2[s*p + c] holds ||B - K X||^2 / ||B||^2 (0 for zero columns) and
-// state[s*p + c] the outcome (LAPY_OK or a negative status).  `skip_seg`
-// (device, nseg, may be null) marks segments whose rows are left untouched.
+// state[s*p + c] the outcome (LAPY_OK or a negative status).
 int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, double* X,
              double rtol, int maxiter, int mixed, double inner_rtol, int max_rounds, void* ws,
              size_t ws_bytes, cudaStream_t stream, IrStats* stats, double* relres2_host,
