@@ -14,6 +14,7 @@
 // part of shared memory with coalesced loads before the per-row gathers.
 // Barriers spin with a bound (common.cuh).
 #include <climits>
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 #include "pcg.cuh"
@@ -121,8 +122,13 @@ int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream) {
   return LAPY_OK;
 }
 
+// Scalar (dot product) type: FP32 for FP32 iterations, FP64 for FP64 ones.
+template <typename V>
+using ScalarOf = typename std::conditional<sizeof(V) == 4, float, double>::type;
+
 template <typename V>
 struct PcgArgs {
+  using S = ScalarOf<V>;
   int64_t n;
   const int32_t* indptr;
   const int32_t* indices;
@@ -143,15 +149,15 @@ struct PcgArgs {
   V* Q;
   V* Z;
   V* T;
-  double* part;       // [3][npiece][NP]  pq, rz, rr
-  double* rz;         // [2][nseg][NP]
-  double* bb;         // [nseg][NP]
+  S* part;            // [3][npiece][NP]  pq, rz, rr
+  S* rz;              // [2][nseg][NP]
+  S* bb;              // [nseg][NP]
   int32_t* state;     // [2][nseg][NP]
   int32_t* state_out; // [nseg][NP]
   unsigned* active;   // [2]
   int* iters;         // [1]
   unsigned long long* work;  // [2] rows and nonzeros processed by the SpMM phase
-  double rtol2;
+  S rtol2;
   int maxiter;
   GridBarrier bar;
 };
@@ -201,12 +207,13 @@ __device__ __forceinline__ void store_row(V* __restrict__ base, int64_t row, con
 }
 
 // Sum of a segment's piece slots for every column; afterwards each lane holds
-// all NP totals in tot[] (fixed summation order).
-template <int NP>
-__device__ __forceinline__ void seg_totals(const double* __restrict__ part, int p0, int p1, double (&tot)[NP]) {
+// all NP totals in tot[] (fixed summation order).  FP32 throughout: the
+// iteration's vectors are FP32, and FP64 arithmetic is scarce on this part.
+template <int NP, typename S>
+__device__ __forceinline__ void seg_totals(const S* __restrict__ part, int p0, int p1, S (&tot)[NP]) {
   const int lane = threadIdx.x & 31;
   constexpr int SPAN = (NP <= 32) ? 32 / NP : 1;
-  double acc = 0.0;
+  S acc = S(0);
   for (int p = p0 + lane / NP; p < p1; p += SPAN) acc += part[(int64_t)p * NP + (lane % NP)];
 #pragma unroll
   for (int o = 16; o >= NP; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -215,12 +222,12 @@ __device__ __forceinline__ void seg_totals(const double* __restrict__ part, int 
 }
 
 // Warp-reduce per-lane column partials and store them to dst[0..NP).
-template <int NP>
-__device__ __forceinline__ void warp_store_partials(const float (&acc)[NP], double* dst) {
+template <int NP, typename S>
+__device__ __forceinline__ void warp_store_partials(const S (&acc)[NP], S* dst) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int q = 0; q < NP; ++q) {
-    const double v = warp_sum((double)acc[q]);
+    const S v = warp_sum(acc[q]);
     if (lane == q) dst[q] = v;
   }
 }
@@ -234,7 +241,8 @@ template <typename V, int NP, bool DOT>
 __device__ __forceinline__ void unit_spmm(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                                           const V* __restrict__ val, const V* __restrict__ Xin,
                                           V* __restrict__ Y, const V* __restrict__ Wdot, int ur0, int ur1,
-                                          V* __restrict__ wval, int32_t* __restrict__ widx, float (&dacc)[NP]) {
+                                          V* __restrict__ wval, int32_t* __restrict__ widx,
+                                          ScalarOf<V> (&dacc)[NP]) {
   const int lane = threadIdx.x & 31;
   const int32_t k0 = ptr[ur0], k1 = ptr[ur1];
   const bool staged = (k1 - k0) <= kStageWarp;
@@ -266,7 +274,7 @@ __device__ __forceinline__ void unit_spmm(const int32_t* __restrict__ ptr, const
       V w[NP];
       load_row<V, NP>(Wdot, row, w);
 #pragma unroll
-      for (int q = 0; q < NP; ++q) dacc[q] += (float)(w[q] * acc[q]);
+      for (int q = 0; q < NP; ++q) dacc[q] += w[q] * acc[q];
     }
   }
 }
@@ -284,21 +292,22 @@ __device__ __forceinline__ void unit_spmm(const int32_t* __restrict__ ptr, const
 
 template <typename V, int NP, int PC>
 __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
+  using S = ScalarOf<V>;
   __shared__ V sval_all[kWarps * kStageWarp];
   __shared__ int32_t sidx_all[kWarps * kStageWarp];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gw = blockIdx.x * kWarps + warp, nw = gridDim.x * kWarps;
   V* wval = sval_all + warp * kStageWarp;
   int32_t* widx = sidx_all + warp * kStageWarp;
-  double* part_pq = a.part;
-  double* part_rz = a.part + (int64_t)a.npiece * NP;
-  double* part_rr = a.part + 2 * (int64_t)a.npiece * NP;
+  S* part_pq = a.part;
+  S* part_rz = a.part + (int64_t)a.npiece * NP;
+  S* part_rr = a.part + 2 * (int64_t)a.npiece * NP;
 
   // ---- phase 0: X = 0, R = B, P = M^-1 R (Jacobi); partial b'b and r'z
   FOR_MY_PIECES(a, {
-    float bb[NP], rz[NP];
+    S bb[NP], rz[NP];
 #pragma unroll
-    for (int q = 0; q < NP; ++q) { bb[q] = 0.f; rz[q] = 0.f; }
+    for (int q = 0; q < NP; ++q) { bb[q] = S(0); rz[q] = S(0); }
     for (int u = u0; u < u1; ++u) {
       const int row = a.unit_row[u] + lane;
       if (row < a.unit_row[u + 1]) {
@@ -311,18 +320,18 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
         if (PC == kPrecJacobi) {
           const V d = a.pc.dinv[row];
 #pragma unroll
-          for (int q = 0; q < NP; ++q) { z[q] = d * b[q]; rz[q] += (float)(b[q] * z[q]); }
+          for (int q = 0; q < NP; ++q) { z[q] = d * b[q]; rz[q] += b[q] * z[q]; }
           store_row<V, NP>(a.P, row, z);
         }
 #pragma unroll
-        for (int q = 0; q < NP; ++q) bb[q] += (float)(b[q] * b[q]);
+        for (int q = 0; q < NP; ++q) bb[q] += b[q] * b[q];
       }
     }
     warp_store_partials<NP>(bb, part_rr + (int64_t)p * NP);
     if (PC == kPrecJacobi) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
   })
   if (PC == kPrecFactored) {
-    float dummy[NP];
+    S dummy[NP];
     if (!grid_sync(a.bar)) return;
     FOR_MY_PIECES(a, {
       for (int u = u0; u < u1; ++u)
@@ -331,9 +340,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
     })
     if (!grid_sync(a.bar)) return;
     FOR_MY_PIECES(a, {
-      float acc[NP];
+      S acc[NP];
 #pragma unroll
-      for (int q = 0; q < NP; ++q) acc[q] = 0.f;
+      for (int q = 0; q < NP; ++q) acc[q] = S(0);
       for (int u = u0; u < u1; ++u)
         unit_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.P, a.R, a.unit_row[u],
                                a.unit_row[u + 1], wval, widx, acc);
@@ -344,7 +353,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   // ---- segment initialisation (the warp holding a segment's first piece publishes)
   FOR_MY_PIECES(a, {
     if (a.seg_piece[s] == p) {
-      double bb[NP], rz[NP];
+      S bb[NP], rz[NP];
       seg_totals<NP>(part_rr, a.seg_piece[s], a.seg_piece[s + 1], bb);
       seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rz);
 #pragma unroll
@@ -352,8 +361,8 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
         if (lane == q) {
           int32_t st;
           if (!isfinite(bb[q]) || !isfinite(rz[q])) st = LAPY_ERR_NAN;
-          else if (bb[q] == 0.0) st = 0;
-          else if (!(rz[q] > 0.0)) st = LAPY_ERR_BREAKDOWN;
+          else if (bb[q] == S(0)) st = 0;
+          else if (!(rz[q] > S(0))) st = LAPY_ERR_BREAKDOWN;
           else st = kActive;
           a.bb[s * NP + q] = bb[q];
           a.rz[s * NP + q] = rz[q];
@@ -370,8 +379,8 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
     const int par = it & 1;
     const int32_t* st_cur = a.state + par * (int64_t)a.nseg * NP;
     int32_t* st_nxt = a.state + (par ^ 1) * (int64_t)a.nseg * NP;
-    const double* rz_cur = a.rz + par * (int64_t)a.nseg * NP;
-    double* rz_nxt = a.rz + (par ^ 1) * (int64_t)a.nseg * NP;
+    const S* rz_cur = a.rz + par * (int64_t)a.nseg * NP;
+    S* rz_nxt = a.rz + (par ^ 1) * (int64_t)a.nseg * NP;
     const unsigned nact = *((volatile unsigned*)&a.active[par]);
     if (nact == 0 || it >= a.maxiter) break;
 
@@ -379,9 +388,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.active[par ^ 1] = 0u;
     FOR_MY_PIECES(a, {
       const bool any = __any_sync(0xffffffffu, lane < NP && st_cur[s * NP + (lane % NP)] == kActive);
-      float acc[NP];
+      S acc[NP];
 #pragma unroll
-      for (int q = 0; q < NP; ++q) acc[q] = 0.f;
+      for (int q = 0; q < NP; ++q) acc[q] = S(0);
       if (any) {
         for (int u = u0; u < u1; ++u)
           unit_spmm<V, NP, true>(a.indptr, a.indices, a.vals, a.P, a.Q, a.P, a.unit_row[u], a.unit_row[u + 1],
@@ -398,20 +407,20 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
 
     // ---- phase B: alpha, X += alpha P, R -= alpha Q, partial r'r (and r'z for Jacobi)
     FOR_MY_PIECES(a, {
-      double pq[NP];
+      S pq[NP];
       seg_totals<NP>(part_pq, a.seg_piece[s], a.seg_piece[s + 1], pq);
       V alpha[NP];
       bool act[NP];
       bool any = false;
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
-        act[q] = st_cur[s * NP + q] == kActive && pq[q] > 0.0 && isfinite(pq[q]);
+        act[q] = st_cur[s * NP + q] == kActive && pq[q] > S(0) && isfinite(pq[q]);
         alpha[q] = act[q] ? (V)(rz_cur[s * NP + q] / pq[q]) : V(0);
         any |= act[q];
       }
-      float rr[NP], rz[NP];
+      S rr[NP], rz[NP];
 #pragma unroll
-      for (int q = 0; q < NP; ++q) { rr[q] = 0.f; rz[q] = 0.f; }
+      for (int q = 0; q < NP; ++q) { rr[q] = S(0); rz[q] = S(0); }
       if (any) {
         for (int u = u0; u < u1; ++u) {
           const int row = a.unit_row[u] + lane;
@@ -428,8 +437,8 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
                 x[q] = x[q] + alpha[q] * pv[q];
                 r[q] = r[q] - alpha[q] * qv[q];
               }
-              rr[q] += (float)(r[q] * r[q]);
-              if (PC == kPrecJacobi) rz[q] += (float)(r[q] * (d * r[q]));
+              rr[q] += r[q] * r[q];
+              if (PC == kPrecJacobi) rz[q] += r[q] * (d * r[q]);
             }
             store_row<V, NP>(a.X, row, x);
             store_row<V, NP>(a.R, row, r);
@@ -443,7 +452,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
 
     if (PC == kPrecFactored) {
       // ---- phase B2: T = G R ; phase B3: Z = Gt T, partial r'z
-      float dummy[NP];
+      S dummy[NP];
       FOR_MY_PIECES(a, {
         for (int u = u0; u < u1; ++u)
           unit_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.unit_row[u],
@@ -451,9 +460,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
       })
       if (!grid_sync(a.bar)) return;
       FOR_MY_PIECES(a, {
-        float acc[NP];
+        S acc[NP];
 #pragma unroll
-        for (int q = 0; q < NP; ++q) acc[q] = 0.f;
+        for (int q = 0; q < NP; ++q) acc[q] = S(0);
         for (int u = u0; u < u1; ++u)
           unit_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R, a.unit_row[u],
                                  a.unit_row[u + 1], wval, widx, acc);
@@ -464,7 +473,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
 
     // ---- phase C: convergence, beta, P = Z + beta P
     FOR_MY_PIECES(a, {
-      double pq[NP], rzn[NP], rr[NP];
+      S pq[NP], rzn[NP], rr[NP];
       seg_totals<NP>(part_pq, a.seg_piece[s], a.seg_piece[s + 1], pq);
       seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rzn);
       seg_totals<NP>(part_rr, a.seg_piece[s], a.seg_piece[s + 1], rr);
@@ -477,10 +486,10 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
         const int32_t st0 = st_cur[s * NP + q];
         int32_t st = st0;
         if (st0 == kActive) {
-          if (!(pq[q] > 0.0) || !isfinite(pq[q])) st = LAPY_ERR_BREAKDOWN;
+          if (!(pq[q] > S(0)) || !isfinite(pq[q])) st = LAPY_ERR_BREAKDOWN;
           else if (!isfinite(rr[q]) || !isfinite(rzn[q])) st = LAPY_ERR_NAN;
           else if (rr[q] <= a.rtol2 * a.bb[s * NP + q]) st = it + 1;
-          else if (!(rzn[q] > 0.0)) st = LAPY_ERR_BREAKDOWN;
+          else if (!(rzn[q] > S(0))) st = LAPY_ERR_BREAKDOWN;
         }
         act[q] = st == kActive;
         beta[q] = act[q] ? (V)(rzn[q] / rz_cur[s * NP + q]) : V(0);
@@ -603,9 +612,10 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
     a.Z = (V*)w; w += vec;
     a.T = (V*)w; w += vec;
   }
-  a.part = (double*)w; w += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
-  a.rz = (double*)w; w += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
-  a.bb = (double*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
+  using S = ScalarOf<V>;
+  a.part = (S*)w; w += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
+  a.rz = (S*)w; w += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
+  a.bb = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
   a.state = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
   unsigned* ctl = (unsigned*)w;  // active[2], iters, count, gen, err, work[2] (u64)
   a.active = ctl;
@@ -615,7 +625,7 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
   a.bar.err = (int*)(ctl + 5);
   a.work = (unsigned long long*)(ctl + 6);
   a.state_out = state_dev;
-  a.rtol2 = rtol * rtol;
+  a.rtol2 = (S)(rtol * rtol);
   a.maxiter = maxiter;
   LAPY_CUDA_TRY(cudaMemsetAsync(ctl, 0, 64, stream));
   // segments without rows have no piece: they are reported as solved
