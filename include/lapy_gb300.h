@@ -176,6 +176,23 @@ int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices,
                    double inner_rtol, int32_t* status_out, double* relres_out,
                    int64_t* iters_out, void* ws, size_t ws_bytes, void* stream);
 
+/* Allocation-free lapy_pcg_solve (no counterpart in the reference, whose
+ * solves run on the host).  For callers that cannot allocate device memory —
+ * a process whose device memory is reserved by another allocator, a code path
+ * where allocating is not allowed, a plain C caller without a workspace — the
+ * scratch is a static device array of LAPY_STATIC_SCRATCH_BYTES that every
+ * GPU loading the library holds until exit.  Problems needing more scratch
+ * (lapy_pcg_solve_workspace_bytes) are rejected with LAPY_ERR_WORKSPACE.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress)
+ * and should come before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race.  Nothing is allocated or freed. */
+#define LAPY_STATIC_SCRATCH_BYTES ((size_t)32 << 20)
+int lapy_pcg_solve_static(int64_t n, const int32_t* indptr, const int32_t* indices,
+                          const double* k_vals, int64_t nnz, int nseg, const int32_t* seg_row,
+                          int ncol, const double* b, double* x, double rtol, int maxiter,
+                          int mixed, double inner_rtol, int32_t* status_out,
+                          double* relres_out, int64_t* iters_out, void* stream);
+
 /* ---- generalized eigenproblem -------------------------------------------
  * Replaces Solver.eigs (lapy/solver.py:667-716): the k eigenpairs of
  * A x = lambda M x nearest sigma, by block shift-invert Lanczos (block width

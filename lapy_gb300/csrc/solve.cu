@@ -1,5 +1,6 @@
 // Batched linear solves with FP64 iterative refinement around FP32 PCG.
 #include <cmath>
+#include <mutex>
 #include <vector>
 #include "blas.cuh"
 #include "solve.cuh"
@@ -312,4 +313,63 @@ extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* i
   LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
   if (iters_out) *iters_out = total_iters;
   return LAPY_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of lapy_pcg_solve.
+//
+// For callers that cannot allocate device memory: processes whose device
+// memory is fully reserved by another allocator, code paths where a device
+// allocation is not allowed, or plain C callers that do not manage a
+// workspace.  Its scratch is this file-scope device array (held by every GPU
+// that loads the library, until the process exits); its address is looked up
+// once per device with cudaGetSymbolAddress, on the first call made with that
+// device current, so that first call should come before any stream capture.
+// Every call shares the one array and leaves its contents behind; the solve
+// clears everything it needs zeroed itself.  Calls that overlap on the GPU
+// (two streams, or two host threads) race on the array.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_pcg_static_scratch[LAPY_STATIC_SCRATCH_BYTES];
+
+static int static_scratch_address(void** out) {
+  static std::mutex mu;
+  static std::vector<void*> per_device;
+  int dev = 0;
+  LAPY_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)per_device.size() <= dev) per_device.resize(dev + 1, nullptr);
+  if (per_device[dev] == nullptr) {
+    void* ptr = nullptr;
+    LAPY_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_pcg_static_scratch));
+    per_device[dev] = ptr;
+  }
+  *out = per_device[dev];
+  return LAPY_OK;
+}
+
+extern "C" int lapy_pcg_solve_static(int64_t n, const int32_t* indptr, const int32_t* indices,
+                                     const double* k_vals, int64_t nnz, int nseg, const int32_t* seg_row,
+                                     int ncol, const double* b, double* x, double rtol, int maxiter, int mixed,
+                                     double inner_rtol, int32_t* status_out, double* relres_out,
+                                     int64_t* iters_out, void* stream) {
+  if (n <= 0 || !indptr || !indices || !k_vals || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0 ||
+      !b || !x || !(rtol > 0) || maxiter <= 0) {
+    lapy_set_last_message("pcg_solve_static: invalid arguments");
+    return LAPY_ERR_INVALID;
+  }
+  if (seg_row[0] != 0 || seg_row[nseg] != n) {
+    lapy_set_last_message("pcg_solve_static: segment rows must span [0, n)");
+    return LAPY_ERR_INVALID;
+  }
+  const size_t need = lapy_pcg_solve_workspace_bytes(n, nnz, nseg, seg_row, ncol, mixed);
+  if (need == 0 || need > LAPY_STATIC_SCRATCH_BYTES) {
+    lapy_set_last_message("pcg_solve_static: this problem needs %zu bytes of scratch; the static array "
+                          "holds %zu (LAPY_STATIC_SCRATCH_BYTES); use lapy_pcg_solve with a workspace",
+                          need, (size_t)LAPY_STATIC_SCRATCH_BYTES);
+    return LAPY_ERR_WORKSPACE;
+  }
+  void* ws = nullptr;
+  LAPY_TRY(static_scratch_address(&ws));
+  return lapy_pcg_solve(n, indptr, indices, k_vals, nnz, nseg, seg_row, ncol, b, x, rtol, maxiter, mixed,
+                        inner_rtol, status_out, relres_out, iters_out, ws, LAPY_STATIC_SCRATCH_BYTES, stream);
 }
