@@ -6,6 +6,8 @@ exports the C ABI declared in ``include/lapy_gb300.h``; Python binds it with
 ctypes (``lapy_gb300/_lib.py``).
 
 Run as ``python -m lapy_gb300.build`` or through ``__graft_entry__.build()``.
+``LAPY_NVCC_FLAGS`` adds flags to every compile (tuning experiments); objects
+are rebuilt when sources change, so clear ``_build/`` after changing it.
 """
 
 from __future__ import annotations
@@ -52,7 +54,8 @@ def _compile(src: Path, nvcc: str) -> Path:
     deps = [src, *CSRC.glob("*.cuh"), *INCLUDE.glob("*.h")]
     if obj.exists() and obj.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return obj
-    cmd = [nvcc, *ARCH, *COMMON, *EXTRA.get(src.name, []), "-c", str(src), "-o", str(obj)]
+    extra_env = os.environ.get("LAPY_NVCC_FLAGS", "").split()
+    cmd = [nvcc, *ARCH, *COMMON, *EXTRA.get(src.name, []), *extra_env, "-c", str(src), "-o", str(obj)]
     proc = subprocess.run(cmd, capture_output=True, text=True)
     if proc.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src.name}:\n{' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")

@@ -361,6 +361,7 @@ struct EigPtrs {
   int32_t* diag_pos; double* k64; float* k32; double* dinv64; float* dinv32;
   double* basis; double* Y; double* W; double* MW;
   void* ir_ws; size_t ir_bytes;
+  void* sell_mem; size_t sell_bytes;
   double* partial;
   double* H; double* Hsum; double* G; double* R1; double* R2; double* Bm;
   double* T; double* Tc; double* theta; double* S; double* eigw;
@@ -404,6 +405,8 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.MW = (double*)take(8 * n * p);
   e.ir_bytes = ir_workspace_bytes(n, p, P.ct, 1, kPrecJacobi);
   e.ir_ws = take(e.ir_bytes);
+  e.sell_bytes = sell_bytes_bound(nnz, P.ct, sizeof(float));
+  e.sell_mem = take(e.sell_bytes);
   const size_t part_elems = (size_t)P.gt.nchunk * std::max((size_t)lda * p, (size_t)keff * keff);
   e.partial = (double*)take(8 * part_elems);
   e.H = (double*)take(8 * (size_t)ns * lda * p);
@@ -522,6 +525,11 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   SysMatrix K;
   K.n = n; K.nnz = P.nnz; K.indptr = indptr; K.indices = indices;
   K.k64 = e.k64; K.k32 = e.k32; K.dinv64 = e.dinv64; K.dinv32 = e.dinv32;
+  {
+    bool fits = false;
+    LAPY_TRY(build_sell<float>(n, indptr, indices, e.k32, P.ct, e.sell_mem, e.sell_bytes, &K.sell32, &fits, st));
+    if (!fits) K.sell32 = SellMatrix<float>();
+  }
 
   std::vector<int32_t> hact(ns, 1), hnsize(ns, 0);
   LAPY_CUDA_TRY(cudaMemcpyAsync(e.active, hact.data(), 4 * ns, cudaMemcpyHostToDevice, st));

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstring>
 #include "pcg.cuh"
+#include "scan.cuh"
 
 namespace lapy {
 
@@ -133,6 +134,8 @@ struct PcgArgs {
   const int32_t* indptr;
   const int32_t* indices;
   const V* vals;
+  SellMatrix<V> sell;
+  int use_sell;
   PcgPrecondDesc<V> pc;
   const int32_t* unit_row;
   const int32_t* piece_unit;
@@ -279,6 +282,40 @@ __device__ __forceinline__ void unit_spmm(const int32_t* __restrict__ ptr, const
   }
 }
 
+// Y = Mat * Xin on unit u (rows [ur0, ur1), lane = row) from the SELL copy.
+template <typename V, int NP, bool DOT>
+__device__ __forceinline__ void sell_unit_spmm(const SellMatrix<V>& M, const V* __restrict__ Xin,
+                                               V* __restrict__ Y, const V* __restrict__ Wdot, int u, int ur0,
+                                               int ur1, ScalarOf<V> (&dacc)[NP]) {
+  const int lane = threadIdx.x & 31;
+  const int32_t base = M.slice_ptr[u];
+  const int w = (M.slice_ptr[u + 1] - base) >> 5;
+  const int32_t* __restrict__ cp = M.col + base + lane;
+  const V* __restrict__ vp = M.val + base + lane;
+  V acc[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) acc[q] = V(0);
+#pragma unroll 4
+  for (int k = 0; k < w; ++k) {
+    const V a = __ldg(vp + 32 * k);
+    const int32_t c = __ldg(cp + 32 * k);
+    V xr[NP];
+    load_row<V, NP>(Xin, c, xr);
+#pragma unroll
+    for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
+  }
+  const int row = ur0 + lane;
+  if (row < ur1) {
+    store_row<V, NP>(Y, row, acc);
+    if (DOT) {
+      V wv[NP];
+      load_row<V, NP>(Wdot, row, wv);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) dacc[q] += wv[q] * acc[q];
+    }
+  }
+}
+
 // Loop over this warp's pieces: s = segment, [u0, u1) = units of the piece.
 #define FOR_MY_PIECES(a, ...)                                                               \
   for (int vw = gw; vw < (a).nvw; vw += nw) {                                                \
@@ -392,9 +429,14 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
 #pragma unroll
       for (int q = 0; q < NP; ++q) acc[q] = S(0);
       if (any) {
-        for (int u = u0; u < u1; ++u)
-          unit_spmm<V, NP, true>(a.indptr, a.indices, a.vals, a.P, a.Q, a.P, a.unit_row[u], a.unit_row[u + 1],
-                                 wval, widx, acc);
+        if (a.use_sell) {
+          for (int u = u0; u < u1; ++u)
+            sell_unit_spmm<V, NP, true>(a.sell, a.P, a.Q, a.P, u, a.unit_row[u], a.unit_row[u + 1], acc);
+        } else {
+          for (int u = u0; u < u1; ++u)
+            unit_spmm<V, NP, true>(a.indptr, a.indices, a.vals, a.P, a.Q, a.P, a.unit_row[u], a.unit_row[u + 1],
+                                   wval, widx, acc);
+        }
         if (lane == 0) {
           const int r0 = a.unit_row[u0], r1 = a.unit_row[u1];
           atomicAdd(&a.work[0], (unsigned long long)(r1 - r0));
@@ -538,6 +580,86 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) a.iters[0] = it;
 }
 
+// ---- sliced-ELL construction ---------------------------------------------
+__global__ void sell_width_kernel(int nunit, const int32_t* __restrict__ unit_row, const int32_t* __restrict__ indptr,
+                                  int32_t* __restrict__ slice_elems) {
+  const int u = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (u >= nunit) return;
+  const int r = unit_row[u] + lane;
+  const int len = (r < unit_row[u + 1]) ? indptr[r + 1] - indptr[r] : 0;
+  const int w = warp_max(len);
+  if (lane == 0) slice_elems[u] = 32 * w;
+}
+
+template <typename V>
+__global__ void sell_fill_kernel(int nunit, const int32_t* __restrict__ unit_row, const int32_t* __restrict__ indptr,
+                                 const int32_t* __restrict__ indices, const V* __restrict__ vals,
+                                 const int32_t* __restrict__ slice_ptr, int32_t* __restrict__ col,
+                                 V* __restrict__ val) {
+  const int u = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (u >= nunit) return;
+  const int r0 = unit_row[u];
+  const int r = r0 + lane;
+  const bool valid = r < unit_row[u + 1];
+  const int32_t kb = valid ? indptr[r] : 0, len = valid ? indptr[r + 1] - kb : 0;
+  const int32_t base = slice_ptr[u];
+  const int w = (slice_ptr[u + 1] - base) >> 5;
+  for (int k = 0; k < w; ++k) {
+    const int32_t pos = base + 32 * k + lane;
+    if (k < len) {
+      col[pos] = indices[kb + k];
+      val[pos] = vals[kb + k];
+    } else {
+      col[pos] = valid ? r : r0;
+      val[pos] = V(0);
+    }
+  }
+}
+
+size_t sell_bytes_bound(int64_t nnz, const ChunkTable& ct, int elem_size) {
+  const size_t elems = (size_t)(1.5 * (double)nnz) + 64 * (size_t)ct.nunit;
+  return a256(4 * (size_t)(ct.nunit + 1)) + a256(4 * (size_t)scan_scratch_elems(ct.nunit + 1)) +
+         a256(4 * (size_t)(ct.nunit + 1)) + a256(4 * elems) + a256((size_t)elem_size * elems) + 256;
+}
+
+template <typename V>
+int build_sell(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals, const ChunkTable& ct,
+               void* mem, size_t bytes, SellMatrix<V>* out, bool* fits, cudaStream_t stream) {
+  (void)n;
+  *fits = false;
+  if (bytes < sell_bytes_bound(0, ct, sizeof(V))) return LAPY_OK;
+  char* w = (char*)(((uintptr_t)mem + 255) & ~uintptr_t(255));
+  char* end = (char*)mem + bytes;
+  int32_t* counts = (int32_t*)w; w += a256(4 * (size_t)(ct.nunit + 1));
+  int32_t* scratch = (int32_t*)w; w += a256(4 * (size_t)scan_scratch_elems(ct.nunit + 1));
+  int32_t* slice_ptr = (int32_t*)w; w += a256(4 * (size_t)(ct.nunit + 1));
+  const unsigned blocks = lapy_ceil_div((int64_t)ct.nunit * 32, 256);
+  sell_width_kernel<<<blocks, 256, 0, stream>>>(ct.nunit, ct.unit_row, indptr, counts);
+  LAPY_TRY(lapy_check_launch("sell_width_kernel"));
+  LAPY_TRY(exclusive_scan_i32(counts, slice_ptr, ct.nunit, scratch, stream));
+  int32_t total = 0;
+  LAPY_CUDA_TRY(cudaMemcpyAsync(&total, slice_ptr + ct.nunit, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+  const size_t need = a256(4 * (size_t)total) + a256(sizeof(V) * (size_t)total);
+  if ((size_t)(end - w) < need || total < 0) return LAPY_OK;  // too much padding: the CSR path is used
+  int32_t* col = (int32_t*)w; w += a256(4 * (size_t)total);
+  V* val = (V*)w;
+  sell_fill_kernel<V><<<blocks, 256, 0, stream>>>(ct.nunit, ct.unit_row, indptr, indices, vals, slice_ptr, col, val);
+  LAPY_TRY(lapy_check_launch("sell_fill_kernel"));
+  out->slice_ptr = slice_ptr;
+  out->col = col;
+  out->val = val;
+  *fits = true;
+  return LAPY_OK;
+}
+
+template int build_sell<float>(int64_t, const int32_t*, const int32_t*, const float*, const ChunkTable&, void*,
+                               size_t, SellMatrix<float>*, bool*, cudaStream_t);
+template int build_sell<double>(int64_t, const int32_t*, const int32_t*, const double*, const ChunkTable&, void*,
+                                size_t, SellMatrix<double>*, bool*, cudaStream_t);
+
 size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond) {
   const size_t vec = a256((size_t)n * p * elem_size);
   size_t b = vec * (precond == kPrecFactored ? 5 : 3);  // R P Q (+ Z T)
@@ -581,8 +703,8 @@ static int launch_pcg_np(PcgArgs<V>& args, int p, cudaStream_t stream) {
 
 template <typename V>
 int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals,
-              const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct, const V* B, V* X,
-              double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
+              const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
+              const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
               cudaStream_t stream, int* iters_out) {
   if (ws_bytes < pcg_workspace_bytes(n, p, ct, sizeof(V), pc.kind)) return LAPY_ERR_WORKSPACE;
   char* w = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
@@ -592,6 +714,8 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
   a.indptr = indptr;
   a.indices = indices;
   a.vals = vals;
+  a.use_sell = sell != nullptr && sell->val != nullptr;
+  if (a.use_sell) a.sell = *sell;
   a.pc = pc;
   a.unit_row = ct.unit_row;
   a.piece_unit = ct.piece_unit;
@@ -665,10 +789,10 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
   return LAPY_OK;
 }
 
-template int pcg_solve<float>(int64_t, const int32_t*, const int32_t*, const float*,
+template int pcg_solve<float>(int64_t, const int32_t*, const int32_t*, const float*, const SellMatrix<float>*,
                               const PcgPrecondDesc<float>&, int, const ChunkTable&, const float*,
                               float*, double, int, int32_t*, void*, size_t, cudaStream_t, int*);
-template int pcg_solve<double>(int64_t, const int32_t*, const int32_t*, const double*,
+template int pcg_solve<double>(int64_t, const int32_t*, const int32_t*, const double*, const SellMatrix<double>*,
                                const PcgPrecondDesc<double>&, int, const ChunkTable&, const double*,
                                double*, double, int, int32_t*, void*, size_t, cudaStream_t, int*);
 

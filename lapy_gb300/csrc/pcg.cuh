@@ -43,6 +43,26 @@ int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream);
 
 enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1 };
 
+// Sliced-ELL copy of a CSR matrix: one slice per 32-row unit of a chunk
+// table, entries stored slot-major inside a slice (element k of the slice's
+// row `lane` at slice_ptr[u] + 32 k + lane), rows padded to the slice's
+// longest row with zero values (column = a row of the slice).  Lane j of a
+// warp reads its row with fully coalesced loads and no per-row pointers.
+template <typename V>
+struct SellMatrix {
+  const int32_t* slice_ptr = nullptr;  // nunit + 1 element offsets
+  const int32_t* col = nullptr;
+  const V* val = nullptr;
+};
+// Workspace reserved for a SELL copy: values and columns for up to
+// 1.5 nnz + 64 entries per unit (mesh matrices pad by a few percent).
+size_t sell_bytes_bound(int64_t nnz, const ChunkTable& ct, int elem_size);
+// Build the SELL copy into `mem`; *fits = false (and no copy) when the padded
+// matrix exceeds the reserved space.
+template <typename V>
+int build_sell(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals, const ChunkTable& ct,
+               void* mem, size_t bytes, SellMatrix<V>* out, bool* fits, cudaStream_t stream);
+
 // Preconditioner description.  Jacobi: z = dinv .* r.  Factored:
 // z = Gt * (G * r) with G, Gt CSR on the mesh pattern (SPD by construction).
 template <typename V>
@@ -64,10 +84,12 @@ size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size
 //   > 0  converged after that many iterations (1-based)
 //   0    x = 0 was exact (zero right-hand side)
 //   < 0  LAPY_ERR_NOCONV / LAPY_ERR_BREAKDOWN / LAPY_ERR_NAN
+// `sell` (may be null) is a SELL copy of the same matrix; when given, the
+// SpMM phase reads it instead of the CSR arrays.
 template <typename V>
 int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals,
-              const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct, const V* B, V* X,
-              double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
+              const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
+              const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
               cudaStream_t stream, int* iters_out);
 
 }  // namespace lapy

@@ -63,7 +63,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
     PcgPrecondDesc<double> pc;
     pc.kind = kPrecJacobi;
     pc.dinv = K.dinv64;
-    LAPY_TRY(pcg_solve<double>(n, K.indptr, K.indices, K.k64, pc, p, ct, B, X, rtol, maxiter, st, pws,
+    LAPY_TRY(pcg_solve<double>(n, K.indptr, K.indices, K.k64, nullptr, pc, p, ct, B, X, rtol, maxiter, st, pws,
                                pws_bytes, stream, &it));
     local.rounds = 1;
     local.pcg_iters = it;
@@ -97,8 +97,8 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
       int it = 0;
       PcgPrecondDesc<float> pc = K.pc32;
       if (pc.kind == kPrecJacobi) pc.dinv = K.dinv32;
-      LAPY_TRY(pcg_solve<float>(n, K.indptr, K.indices, K.k32, pc, p, ct, R32, D32, round_rtol, maxiter,
-                                st, pws, pws_bytes, stream, &it));
+      LAPY_TRY(pcg_solve<float>(n, K.indptr, K.indices, K.k32, K.sell32.val ? &K.sell32 : nullptr, pc, p, ct, R32,
+                                D32, round_rtol, maxiter, st, pws, pws_bytes, stream, &it));
       local.rounds++;
       local.pcg_iters += it;
       LAPY_TRY(add_f32_to_f64(n * p, D32, X, stream));
@@ -209,7 +209,8 @@ static int next_pow2_le16(int c) {
 static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed, char* base,
                            int32_t** diag_pos, double** dinv64, float** dinv32, float** k32,
                            double** Bp, double** Xp, void** chunk_mem, void** ir_ws, size_t* ir_bytes,
-                           int* nchunk_out, ChunkTable* ct_plan, const int32_t* seg_row) {
+                           void** sell_mem, size_t* sell_bytes, int* nchunk_out, ChunkTable* ct_plan,
+                           const int32_t* seg_row) {
   const int w = std::min(ncol, 16);
   const int p = next_pow2_le16(w);
   ChunkTable ct;
@@ -230,6 +231,8 @@ static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed
   char* p6 = take(chunk_table_bytes(ct));
   const size_t irb = ir_workspace_bytes(n, p, ct, mixed, kPrecJacobi);
   char* p7 = take(irb);
+  const size_t sellb = mixed ? sell_bytes_bound(nnz, ct, sizeof(float)) : 0;
+  char* p8 = take(sellb);
   if (base) {
     *diag_pos = (int32_t*)p0;
     *dinv64 = (double*)p1;
@@ -240,6 +243,8 @@ static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed
     *chunk_mem = p6;
     *ir_ws = p7;
     *ir_bytes = irb;
+    *sell_mem = p8;
+    *sell_bytes = sellb;
     *nchunk_out = ct.nchunk;
     *ct_plan = ct;
   }
@@ -250,7 +255,7 @@ extern "C" size_t lapy_pcg_solve_workspace_bytes(int64_t n, int64_t nnz, int nse
                                                  int ncol, int mixed) {
   if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0) return 0;
   return solve_layout(n, nnz, nseg, ncol, mixed, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                      nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row);
+                      nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row);
 }
 
 extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices,
@@ -272,13 +277,13 @@ extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* i
   int32_t* diag_pos;
   double *dinv64, *Bp, *Xp;
   float *dinv32, *k32;
-  void *chunk_mem, *ir_ws;
-  size_t ir_bytes;
+  void *chunk_mem, *ir_ws, *sell_mem;
+  size_t ir_bytes, sell_bytes;
   int nchunk;
   ChunkTable ct;
   char* base = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
   solve_layout(n, nnz, nseg, ncol, mixed, base, &diag_pos, &dinv64, &dinv32, &k32, &Bp, &Xp, &chunk_mem,
-               &ir_ws, &ir_bytes, &nchunk, &ct, seg_row);
+               &ir_ws, &ir_bytes, &sell_mem, &sell_bytes, &nchunk, &ct, seg_row);
   LAPY_TRY(upload_chunk_table(&ct, chunk_mem, stream));
   LAPY_TRY(lapy_csr_diag_index(n, indptr, indices, diag_pos, stream));
   LAPY_TRY(jacobi_inverse(n, diag_pos, k_vals, dinv64, dinv32, stream));
@@ -292,6 +297,11 @@ extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* i
   K.k32 = k32;
   K.dinv64 = dinv64;
   K.dinv32 = dinv32;
+  if (mixed) {
+    bool fits = false;
+    LAPY_TRY(build_sell<float>(n, indptr, indices, k32, ct, sell_mem, sell_bytes, &K.sell32, &fits, stream));
+    if (!fits) K.sell32 = SellMatrix<float>();
+  }
   int64_t total_iters = 0;
   for (int c0 = 0; c0 < ncol; c0 += 16) {
     const int w = std::min(16, ncol - c0);

@@ -15,6 +15,7 @@ struct SysMatrix {
   const double* dinv64 = nullptr;
   const float* dinv32 = nullptr;
   PcgPrecondDesc<float> pc32;  // kind == kPrecFactored selects the learned/SPAI factor
+  SellMatrix<float> sell32;    // SELL copy of k32 (val == nullptr: CSR path)
 };
 
 struct IrStats {
