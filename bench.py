@@ -11,6 +11,13 @@ CSR) + the batched block shift-invert Lanczos solve, with the meshes resident
 in HBM (``value``).  ``e2e`` runs the public API (``compute_shapedna_batch``)
 from host arrays: mesh upload, assembly, eigensolve, eigenvalue download.
 
+The same line carries the second half of the metric, ``heat``: heat solves/s
+on the same batch (one backward-Euler step (M_s + t_s A_s) u = e_0 per mesh,
+lumped mass, t_s = mean edge length squared, lapy/heat.py:114-232), resident
+and end to end.  ``plain`` legs time the unbatched GPU method (one mesh at a
+time through ``Solver.eigs`` / ``heat.diffusion``, Jacobi-PCG) on a stratified
+sample, so that batched vs plain is measured in the same run.
+
 ``--impl reference`` times the reference's CPU method (SciPy splu + eigsh, the
 oracle's restatement of lapy/solver.py) on a stratified sample of the same
 meshes with all host cores.
@@ -61,6 +68,38 @@ def make_batch(n_meshes: int, seed: int, levels=(3, 4, 5, 6)):
         r = 1.0 + 0.1 * (Y @ c)
         out.append(TriaMesh(u * r[:, None], base[L].t))
     return out, lv
+
+
+def rank_seed(seed: int, rank: int) -> int:
+    """Each rank solves its own shard of meshes (independent units, no exchange)."""
+    return seed + 7919 * rank
+
+
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """Slowest rank's time: the job is done when every shard is done."""
+    if world <= 1:
+        return x
+    import torch
+
+    tt = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def stratified(lv, per_level: int):
+    idx = []
+    for L in sorted(set(lv.tolist())):
+        idx += [i for i in range(len(lv)) if lv[i] == L][:per_level]
+    return idx
+
+
+def extrapolate(lv, idx, secs):
+    """Whole-batch seconds from per-level mean seconds of a sample."""
+    per_level_s = {}
+    for i, s_ in zip(idx, secs):
+        per_level_s.setdefault(int(lv[i]), []).append(s_)
+    total = sum(float(np.mean(per_level_s[int(L)])) for L in lv.tolist())
+    return total, {str(k): float(np.mean(v)) for k, v in per_level_s.items()}
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -117,17 +156,18 @@ def _cpu_one(args):
     t0 = time.perf_counter()
     A, M = oracle.assemble_scipy(v, t)
     ev, _ = oracle.eigs(A, M, k=k)
-    return time.perf_counter() - t0
+    t1 = time.perf_counter()
+    oracle.diffusion(v, t, 0, m=1.0)
+    return t1 - t0, time.perf_counter() - t1
 
 
 def cpu_baseline(meshes, lv, per_level: int = 4, cores: int | None = None):
-    """Reference CPU method (assembly + splu/eigsh) on a stratified sample, all cores."""
+    """Reference CPU method (assembly + splu/eigsh; splu heat step) on a
+    stratified sample, all cores.  Returns (spectra baseline, heat baseline)."""
     import multiprocessing as mp
 
     cores = cores or len(os.sched_getaffinity(0))
-    idx = []
-    for L in sorted(set(lv.tolist())):
-        idx += [i for i in range(len(meshes)) if lv[i] == L][:per_level]
+    idx = stratified(lv, per_level)
     work = [(meshes[i].v, meshes[i].t, K_EIG) for i in idx]
     env = {"OPENBLAS_NUM_THREADS": "1", "OMP_NUM_THREADS": "1", "MKL_NUM_THREADS": "1"}
     old = {k: os.environ.get(k) for k in env}
@@ -148,16 +188,16 @@ def cpu_baseline(meshes, lv, per_level: int = 4, cores: int | None = None):
     # Throughput on the whole batch: mean CPU seconds per mesh of each level
     # (measured on the sample, one mesh per worker process) times the batch's
     # level counts, spread over all cores.
-    per_level_s = {}
-    for i, s in zip(idx, secs):
-        per_level_s.setdefault(int(lv[i]), []).append(s)
-    total = sum(float(np.mean(per_level_s[int(L)])) for L in lv.tolist())
-    value = len(meshes) / (total / cores)
-    return {"value": value, "unit": "spectra/s", "cores": cores, "kind": "port",
-            "sample": f"{len(work)} meshes ({per_level} per icosphere level 3-6) timed one per worker "
-                      f"(BLAS threads 1, sample wall {wall:.1f} s); the batch's CPU seconds "
-                      f"({total:.0f}) spread over {cores} cores",
-            "sec_per_mesh_by_level": {str(k): float(np.mean(v)) for k, v in per_level_s.items()}}
+    total, by_level = extrapolate(lv, idx, [e for e, _ in secs])
+    total_h, by_level_h = extrapolate(lv, idx, [h for _, h in secs])
+    sample = (f"{len(work)} meshes ({per_level} per icosphere level 3-6) timed one per worker "
+              f"(BLAS threads 1, sample wall {wall:.1f} s); the batch's CPU seconds "
+              f"({{:.0f}}) spread over {cores} cores")
+    spectra = {"value": len(meshes) / (total / cores), "unit": "spectra/s", "cores": cores, "kind": "port",
+               "sample": sample.format(total), "sec_per_mesh_by_level": by_level}
+    heat = {"value": len(meshes) / (total_h / cores), "unit": "heat solves/s", "cores": cores, "kind": "port",
+            "sample": sample.format(total_h) + " (splu of M + t A, lumped M)", "sec_per_mesh_by_level": by_level_h}
+    return spectra, heat
 
 
 # ----------------------------------------------------------------------------- GPU arm
@@ -175,7 +215,7 @@ def run_gpu(args, rank, world):
     from lapy_gb300 import _lib, shapedna
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-    meshes, lv = make_batch(args.meshes, seed=args.seed + 7919 * rank)
+    meshes, lv = make_batch(args.meshes, seed=rank_seed(args.seed, rank))
     # inputs resident in HBM before the timed region
     batch_in = shapedna.BatchInput(meshes)
     torch.cuda.synchronize()
@@ -210,16 +250,12 @@ def run_gpu(args, rank, world):
     prof = _lib.profile_read()
     launches = _lib.launch_count() - L0
     dev_s = ev0.elapsed_time(ev1) / 1e3
-    t_max = dev_s
-    if world > 1:
-        tt = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = max_over_ranks(dev_s, world)
     status_ok = all(int(s) == 0 for inf in infos for s in inf["status"])
 
     # e2e through the public API from host buffers
     torch.cuda.synchronize()
-    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 2))
+    e2e_steps = 0 if args.no_e2e else 1
     te = time.perf_counter()
     for _ in range(e2e_steps):
         res = shapedna.compute_shapedna_batch(meshes, k=K_EIG, block=args.block, return_vectors=False)
@@ -254,9 +290,98 @@ def run_gpu(args, rank, world):
         "pcg": {k: prof[k] for k in ("pcg_launches", "pcg_iterations", "rows", "nnz")},
         "wall_s": wall,
     }
+    if not args.no_heat:
+        line["heat"] = run_heat(args, meshes, lv, batch_in, world)
+    if not args.no_plain:
+        line["plain"] = run_plain_spectra(args, meshes, lv, line["value"] / world)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
+        line["cpu_baseline"], heat_cpu = cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
+        if "heat" in line:
+            line["heat"]["cpu_baseline"] = heat_cpu
     return line
+
+
+def _timed(fn, steps, warmup):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(steps):
+        fn()
+    ev1.record()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3
+
+
+def run_heat(args, meshes, lv, batch_in, world):
+    """Heat solves/s: batched (resident and end to end) and plain (per mesh)."""
+    import torch
+
+    from lapy_gb300 import heat
+
+    hb = heat.HeatBatch(batch_in, vids=0, m=1.0)
+    out = {}
+
+    def step():
+        x, info = hb.solve()
+        out["info"] = info
+
+    dev_s = max_over_ranks(_timed(step, args.steps, args.warmup), world)
+    relres = float(np.max(out["info"]["relres"]))
+    te = time.perf_counter()
+    if not args.no_e2e:
+        heat.diffusion_batch(meshes, 0, m=1.0)
+        torch.cuda.synchronize()
+    te = time.perf_counter() - te
+    # plain: the unbatched API, one mesh at a time
+    idx = stratified(lv, args.plain_per_level)
+    heat.diffusion(meshes[idx[0]], 0)  # warm
+    secs = []
+    for i in idx:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        heat.diffusion(meshes[i], 0)
+        torch.cuda.synchronize()
+        secs.append(time.perf_counter() - t0)
+    total, by_level = extrapolate(lv, idx, secs)
+    value = world * args.meshes * args.steps / dev_s
+    plain = args.meshes / total
+    return {"value": value, "unit": "heat solves/s", "ms_per_step": dev_s * 1e3 / args.steps,
+            "max_relres": relres, "pcg_iterations": int(out["info"]["iters"]),
+            "e2e": ({"value": world * args.meshes / te, "unit": "heat solves/s",
+                     "h2d_bytes_per_step": sum(m.v.nbytes + m.t.size * 4 for m in meshes) + 8 * len(meshes),
+                     "d2h_bytes_per_step": 8 * sum(len(m.v) for m in meshes)} if not args.no_e2e else None),
+            "plain": {"value": world * plain, "unit": "heat solves/s",
+                      "sample": f"{len(idx)} meshes ({args.plain_per_level} per level) through heat.diffusion one "
+                                f"at a time, extrapolated by level counts", "sec_per_mesh_by_level": by_level},
+            "vs_plain": value / (world * plain)}
+
+
+def run_plain_spectra(args, meshes, lv, batched_per_gpu):
+    """The unbatched GPU method: Solver(mesh).eigs(50) one mesh at a time."""
+    import torch
+
+    from lapy_gb300 import Solver
+
+    idx = stratified(lv, args.plain_per_level)
+    Solver(meshes[idx[0]]).eigs(k=K_EIG)  # warm
+    secs = []
+    for i in idx:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Solver(meshes[i]).eigs(k=K_EIG)
+        torch.cuda.synchronize()
+        secs.append(time.perf_counter() - t0)
+    total, by_level = extrapolate(lv, idx, secs)
+    plain = args.meshes / total
+    return {"value": plain, "unit": "spectra/s", "per_gpu": True,
+            "sample": f"{len(idx)} meshes ({args.plain_per_level} per level) through Solver(mesh).eigs(50) one at a "
+                      f"time (Jacobi-PCG), extrapolated by level counts", "sec_per_mesh_by_level": by_level,
+            "vs_plain": batched_per_gpu / plain}
 
 
 def run_reference(args):
@@ -264,10 +389,14 @@ def run_reference(args):
     vals = []
     for _ in range(args.warmup):
         pass  # the CPU method has no warm-up state beyond imports (done in the pool)
+    heats = []
     for _ in range(args.steps):
-        vals.append(cpu_baseline(meshes, lv, per_level=args.cpu_per_level))
+        sp, ht = cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
+        vals.append(sp)
+        heats.append(ht)
     v = statistics.median([x["value"] for x in vals])
     base = vals[0]
+    hv = statistics.median([x["value"] for x in heats])
     return {"metric": METRIC, "value": v, "unit": "spectra/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * (args.cpu_per_level * 4) / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -275,20 +404,24 @@ def run_reference(args):
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "spectra/s", "cores": base["cores"], "kind": "port",
                              "sample": base["sample"]},
-            "e2e": {"value": v, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "heat": {"value": hv, "unit": "heat solves/s", "cpu_baseline": heats[0]}}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--meshes", type=int, default=512)
     ap.add_argument("--block", type=int, default=2)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-per-level", type=int, default=4)
+    ap.add_argument("--plain-per-level", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-heat", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the public-API end-to-end leg (profiling runs)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))

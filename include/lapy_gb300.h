@@ -130,6 +130,13 @@ int lapy_avg_edge_length(const void* v, int coords_f32, int64_t n, const int32_t
                          const int32_t* indices, double* out, void* work,
                          size_t ws_bytes, void* stream);
 size_t lapy_avg_edge_length_workspace_bytes(int64_t n);
+/* Batched form: out[s] (device, nseg doubles) = mean edge length of segment s
+ * of a block-diagonal batch (seg_row: device, nseg+1 row offsets); t_out
+ * (device, may be NULL) receives each mesh's heat time step
+ * t = m * avg_edge_length**2 (lapy/heat.py:206). */
+int lapy_seg_avg_edge_length(const void* v, int coords_f32, int nseg, const int32_t* seg_row,
+                             const int32_t* indptr, const int32_t* indices, double m, double* out,
+                             double* t_out, void* stream);
 
 /* ---- sparse matrix-vector products -------------------------------------
  * Y = alpha * Mat * X + beta * Y for X, Y row-major n x ncol.  Used wherever
@@ -150,6 +157,14 @@ int lapy_diag_mm_f64(int64_t n, const double* d, int ncol, const double* x, doub
  * and A - sigma*M (lapy/solver.py:707) on a shared pattern. */
 int lapy_vec_axpby(int64_t n, double a, const double* x, double b, const double* y,
                    double* out, void* stream);
+/* Batched form of hmat = M + t*A (lapy/heat.py:208) with one coefficient pair
+ * per segment: out = alpha[s]*x + beta[s]*y on the rows of segment s
+ * (seg_row, alpha, beta: device arrays).  y_is_diag: y is an n-vector added
+ * at diag_pos (a lumped mass). */
+int lapy_csr_seg_axpby(int nseg, const int32_t* seg_row, const int32_t* indptr,
+                       const int32_t* diag_pos, const double* alpha, const double* x,
+                       const double* beta, const double* y, int y_is_diag, double* out,
+                       void* stream);
 /* vals[diag_pos[i]] += b * d[i]: adds a lumped (diagonal) mass to a matrix. */
 int lapy_csr_add_diag(int64_t n, const int32_t* diag_pos, double b, const double* d,
                       double* vals, void* stream);

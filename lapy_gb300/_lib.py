@@ -69,6 +69,8 @@ _SIGNATURES = {
     "lapy_csr_pattern_map": (_int, [_i64, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
     "lapy_avg_edge_length": (_int, [_vp, _int, _i64, _vp, _vp, C.POINTER(_dbl), _vp, _sz, _vp]),
     "lapy_avg_edge_length_workspace_bytes": (_sz, [_i64]),
+    "lapy_seg_avg_edge_length": (_int, [_vp, _int, _int, _vp, _vp, _vp, _dbl, _vp, _vp, _vp]),
+    "lapy_csr_seg_axpby": (_int, [_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _vp, _vp]),
     "lapy_csr_spmm_f64": (_int, [_i64, _vp, _vp, _vp, _int, _vp, _vp, _dbl, _dbl, _int, _vp]),
     "lapy_csr_spmm_f32": (_int, [_i64, _vp, _vp, _vp, _int, _vp, _vp, C.c_float, C.c_float, _int, _vp]),
     "lapy_diag_mm_f64": (_int, [_i64, _vp, _int, _vp, _vp, _dbl, _dbl, _vp]),

@@ -87,9 +87,83 @@ __global__ void edge_len_final_kernel(const double* psum, const long long* pcnt,
   if (threadIdx.x == 0) out[0] = c ? s / (double)c : 0.0;
 }
 
+// One CTA per segment: mean edge length of the segment's strict upper
+// triangle, summed in a fixed order (thread-strided rows, then block_sum).
+template <typename T>
+__global__ void seg_edge_len_kernel(const T* __restrict__ v, const int32_t* __restrict__ seg_row,
+                                    const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                    double m, double* __restrict__ out, double* __restrict__ t_out) {
+  __shared__ double sh[32];
+  __shared__ long long shc[32];
+  const int s = blockIdx.x;
+  double acc = 0.0;
+  long long c = 0;
+  for (int64_t r = seg_row[s] + threadIdx.x; r < seg_row[s + 1]; r += blockDim.x) {
+    const T x0 = v[3 * r], y0 = v[3 * r + 1], z0 = v[3 * r + 2];
+    for (int32_t k = indptr[r]; k < indptr[r + 1]; ++k) {
+      const int32_t j = indices[k];
+      if (j <= r) continue;
+      const T dx = x0 - v[3 * (int64_t)j], dy = y0 - v[3 * (int64_t)j + 1], dz = z0 - v[3 * (int64_t)j + 2];
+      T q = dx * dx;
+      q = q + dy * dy;
+      q = q + dz * dz;
+      acc += (double)sqrt(q);
+      c += 1;
+    }
+  }
+  acc = block_sum(acc, sh);
+  c = block_sum(c, shc);
+  if (threadIdx.x == 0) {
+    const double avg = c ? acc / (double)c : 0.0;
+    out[s] = avg;
+    if (t_out) t_out[s] = __dmul_rn(m, __dmul_rn(avg, avg));  // lapy/heat.py:206
+  }
+}
+
+// out = alpha[s] x + beta[s] y on the rows of segment s (one CTA per
+// segment); y_is_diag: y is an n-vector added at the diagonal positions.
+__global__ void seg_axpby_kernel(const int32_t* __restrict__ seg_row, const int32_t* __restrict__ indptr,
+                                 const int32_t* __restrict__ diag_pos, const double* __restrict__ alpha,
+                                 const double* __restrict__ x, const double* __restrict__ beta,
+                                 const double* __restrict__ y, int y_is_diag, double* __restrict__ out) {
+  const int s = blockIdx.x;
+  const double a = alpha[s], b = beta[s];
+  const int32_t k0 = indptr[seg_row[s]], k1 = indptr[seg_row[s + 1]];
+  for (int32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x)
+    out[k] = y_is_diag ? __dmul_rn(a, x[k]) : __dadd_rn(__dmul_rn(a, x[k]), __dmul_rn(b, y[k]));
+  if (y_is_diag) {
+    __syncthreads();
+    for (int32_t r = seg_row[s] + threadIdx.x; r < seg_row[s + 1]; r += blockDim.x)
+      out[diag_pos[r]] = __dadd_rn(out[diag_pos[r]], __dmul_rn(b, y[r]));
+  }
+}
+
 }  // namespace lapy
 
 using namespace lapy;
+
+extern "C" int lapy_seg_avg_edge_length(const void* v, int coords_f32, int nseg, const int32_t* seg_row,
+                                        const int32_t* indptr, const int32_t* indices, double m, double* out,
+                                        double* t_out, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (!v || nseg <= 0 || !seg_row || !indptr || !indices || !out) return LAPY_ERR_INVALID;
+  if (coords_f32)
+    seg_edge_len_kernel<float><<<nseg, 256, 0, stream>>>((const float*)v, seg_row, indptr, indices, m, out, t_out);
+  else
+    seg_edge_len_kernel<double><<<nseg, 256, 0, stream>>>((const double*)v, seg_row, indptr, indices, m, out, t_out);
+  return lapy_check_launch("seg_edge_len_kernel");
+}
+
+extern "C" int lapy_csr_seg_axpby(int nseg, const int32_t* seg_row, const int32_t* indptr,
+                                  const int32_t* diag_pos, const double* alpha, const double* x,
+                                  const double* beta, const double* y, int y_is_diag, double* out,
+                                  void* stream_) {
+  if (nseg <= 0 || !seg_row || !indptr || !alpha || !x || !beta || !y || !out || (y_is_diag && !diag_pos))
+    return LAPY_ERR_INVALID;
+  seg_axpby_kernel<<<nseg, 256, 0, (cudaStream_t)stream_>>>(seg_row, indptr, diag_pos, alpha, x, beta, y,
+                                                             y_is_diag, out);
+  return lapy_check_launch("seg_axpby_kernel");
+}
 
 extern "C" int lapy_csr_diag_index(int64_t n, const int32_t* indptr, const int32_t* indices,
                                    int32_t* diag_pos, void* stream) {

@@ -14,7 +14,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._device import pcg_solve
+from ._device import dptr, pcg_solve, stream
 
 logger = logging.getLogger(__name__)
 
@@ -60,3 +60,67 @@ def diffusion(geometry, vids, m: float = 1.0, aniso=None, use_cholmod: bool = Fa
     if scalar_input:
         return vfunc[:, 0]
     return vfunc
+
+
+class HeatBatch:
+    """Backward-Euler heat systems of a batch of meshes on the device.
+
+    Each mesh s of the block-diagonal batch gets its own
+    ``t_s = m * avg_edge_length_s**2`` (lapy/heat.py:206) and the system
+    ``(M_s + t_s A_s) u = b0_s`` with lumped ``M`` (lapy/heat.py:204, 208); all
+    segments are solved by one batched PCG launch sequence."""
+
+    def __init__(self, batch_input, vids=0, m: float = 1.0):
+        from .shapedna import BatchInput
+
+        if not isinstance(batch_input, BatchInput):
+            batch_input = BatchInput(batch_input)
+        self.input = batch_input
+        self.m = float(m)
+        seg = batch_input.seg_row
+        nseg = len(seg) - 1
+        sizes = np.diff(seg)
+        v = np.asarray(vids, dtype=np.int64).reshape(-1)
+        if v.size == 1:
+            v = np.full(nseg, v[0])
+        if len(v) != nseg:
+            raise ValueError("vids needs one vertex per mesh (or one vertex for all)")
+        if np.any(v < 0) or np.any(v >= sizes):
+            raise ValueError("vids contains out-of-range vertex indices")
+        b0 = np.zeros(seg[-1])
+        b0[seg[:-1] + v] = 1.0
+        self.b0 = torch.from_numpy(b0).to("cuda")
+        self.ones = torch.ones(nseg, dtype=torch.float64, device="cuda")
+
+    def solve(self, rtol: float = 1e-11, maxiter: int = 20000):
+        """Assemble and solve every segment; returns (u (n,), info)."""
+        from .shapedna import BatchedFEM
+
+        inp = self.input
+        fem = BatchedFEM.from_input(inp, lump=True)
+        L = _lib.lib()
+        nseg = len(inp.seg_row) - 1
+        seg_dev = inp.seg_row_dev
+        avg = torch.empty(nseg, dtype=torch.float64, device="cuda")
+        t = torch.empty(nseg, dtype=torch.float64, device="cuda")
+        _lib.check(L.lapy_seg_avg_edge_length(dptr(inp.mesh.v), inp.mesh.coords_f32, nseg, dptr(seg_dev),
+                                              dptr(fem.indptr), dptr(fem.indices), self.m, dptr(avg), dptr(t),
+                                              stream()), "seg_avg_edge_length")
+        hvals = torch.empty(fem.nnz, dtype=torch.float64, device="cuda")
+        _lib.check(L.lapy_csr_seg_axpby(nseg, dptr(seg_dev), dptr(fem.indptr), dptr(fem.pattern.diag_pos),
+                                        dptr(t), dptr(fem.a_vals), dptr(self.ones), dptr(fem.m_vals), 1,
+                                        dptr(hvals), stream()), "csr_seg_axpby")
+        x, relres, iters = pcg_solve(fem.indptr, fem.indices, hvals, fem.n, fem.nnz, self.b0, rtol, maxiter,
+                                     seg_row=inp.seg_row)
+        return x, {"relres": relres, "iters": iters, "t": t, "avg_edge_length": avg}
+
+
+def diffusion_batch(meshes, vids=0, m: float = 1.0, rtol: float = 1e-11) -> list:
+    """Heat diffusion on many meshes at once: ``diffusion(mesh_s, vids[s], m)``
+    for every mesh, solved as one block-diagonal batch.  ``vids``: one vertex
+    per mesh, or one vertex index used for all meshes."""
+    hb = HeatBatch(meshes, vids, m)
+    x, _ = hb.solve(rtol)
+    u = x.cpu().numpy()
+    seg = hb.input.seg_row
+    return [u[seg[i]:seg[i + 1]] for i in range(len(seg) - 1)]

@@ -64,6 +64,7 @@ class BatchInput:
         t = torch.from_numpy(np.ascontiguousarray(np.concatenate(ts).astype(np.int32))).to("cuda")
         self.mesh = MeshDevice(v, t, seg[-1], seg[-1], t.shape[0], npe)
         self.seg_row = np.array(seg, dtype=np.int32)
+        self.seg_row_dev = torch.from_numpy(self.seg_row).to("cuda")
 
 
 class BatchedFEM:

@@ -194,6 +194,24 @@ def test_heat_parity(cuda_ok, name):
     np.testing.assert_allclose(um[:, 0], u, rtol=1e-7, atol=1e-10 * np.abs(u).max())
 
 
+def test_heat_batch_matches_oracle(cuda_ok):
+    """Batched heat: every mesh its own t = avg_edge_length**2 and seed vertex."""
+    from lapy_gb300 import heat, meshes
+
+    ms = [meshes.sh_deform(meshes.icosphere(lv), seed=s) for lv, s in ((2, 5), (3, 6), (1, 7), (3, 8), (2, 9))]
+    vids = [0, 11, 3, 40, 7]
+    out = heat.diffusion_batch(ms, vids, m=2.0)
+    for mesh, v, u in zip(ms, vids, out):
+        ref = oracle.diffusion(mesh.v, mesh.t, v, m=2.0)
+        _, M = oracle.assemble_scipy(mesh.v, mesh.t, lump=True)
+        assert u.shape == (len(mesh.v),)
+        assert _mnorm_rel(u, ref, M.diagonal()) <= 1e-8
+    with pytest.raises(ValueError, match="out-of-range"):
+        heat.diffusion_batch(ms, [0, 0, 0, 0, len(ms[4].v)])
+    with pytest.raises(ValueError, match="one vertex per mesh"):
+        heat.diffusion_batch(ms, [0, 1])
+
+
 def test_heat_out_of_range_raises(cuda_ok):
     from lapy_gb300 import heat
 
