@@ -216,14 +216,19 @@ int lapy_pcg_solve_static(int64_t n, const int32_t* indptr, const int32_t* indic
  * (m_is_diag == 0, nnz values) or as its diagonal (m_is_diag != 0, n values).
  * evals: device nseg*k (ascending per segment); evecs: device row-major n x k,
  * M-orthonormal per segment.  status_out / nbasis_out: host nseg.
- * tol: Ritz residual tolerance; inner_rtol: inner-solve residual target. */
+ * tol: Ritz residual tolerance; inner_rtol: inner-solve residual target.
+ * precond: preconditioner of the inner PCG, LAPY_PRECOND_JACOBI or
+ * LAPY_PRECOND_TWO_LEVEL (Jacobi plus a per-mesh aggregation coarse space
+ * with a dense coarse inverse; the reference factorises instead, splu). */
+#define LAPY_PRECOND_JACOBI 0
+#define LAPY_PRECOND_TWO_LEVEL 2
 size_t lapy_eigs_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row,
-                                 int k, int block, int max_vectors);
+                                 int k, int block, int max_vectors, int precond);
 int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const int32_t* indices,
                            const double* a_vals, const double* m_vals, int m_is_diag,
                            int64_t nnz, int nseg, const int32_t* seg_row, double sigma, int k,
                            int block, int max_vectors, double tol, double inner_rtol,
-                           int inner_maxiter, uint64_t seed, double* evals, double* evecs,
+                           int inner_maxiter, int precond, uint64_t seed, double* evals, double* evecs,
                            int32_t* status_out, int32_t* nbasis_out, int64_t* inner_iters_out,
                            void* ws, size_t ws_bytes, void* stream);
 

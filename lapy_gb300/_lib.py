@@ -81,13 +81,16 @@ _SIGNATURES = {
                               _vp, _vp, C.POINTER(_i64), _vp, _sz, _vp]),
     "lapy_pcg_solve_static": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _dbl, _int, _int,
                                      _dbl, _vp, _vp, C.POINTER(_i64), _vp]),
-    "lapy_eigs_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int, _int, _int]),
+    "lapy_eigs_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int, _int, _int, _int]),
     "lapy_eigs_shift_invert": (_int, [_i64, _vp, _vp, _vp, _vp, _int, _i64, _int, _vp, _dbl, _int, _int,
-                                      _int, _dbl, _dbl, _int, C.c_uint64, _vp, _vp, _vp, _vp,
+                                      _int, _dbl, _dbl, _int, _int, C.c_uint64, _vp, _vp, _vp, _vp,
                                       C.POINTER(_i64), _vp, _sz, _vp]),
 }
 
 # Optional entry points (present when the matching translation unit is built).
+PRECOND_JACOBI = 0
+PRECOND_TWO_LEVEL = 2
+
 _OPTIONAL = {
     "lapy_csr_dirichlet_mask": (_int, [_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "lapy_tria_gradient": (_int, [_vp, _int, _vp, _i64, _vp, _int, _vp, _vp]),

@@ -1,0 +1,343 @@
+// Two-level (aggregation) preconditioner: coarse space of a block-diagonal
+// batch.
+//
+// Host: each segment's rows are grouped into connected aggregates by
+// breadth-first growth on the matrix graph (deterministic: rows are visited
+// in index order, neighbours in CSR order; segments are independent and run
+// on a fixed set of host threads).  Device: the Galerkin matrix W'KW of every
+// segment (one thread per coarse row, fixed summation order) and its dense
+// inverse (one CTA per segment: FP64 Cholesky, triangular inverse, B'B),
+// stored in FP32 for the per-iteration coarse product of the PCG.
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+#include "coarse.cuh"
+
+namespace lapy {
+
+static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static int64_t seg_cap(int64_t rows) { return rows <= 0 ? 0 : (rows + kAggMinAvg - 1) / kAggMinAvg; }
+
+int64_t two_level_max_aggs(const int32_t* seg_row, int nseg) {
+  int64_t t = 0;
+  for (int s = 0; s < nseg; ++s) t += std::min<int64_t>(seg_cap(seg_row[s + 1] - seg_row[s]), kCoarseMaxDim);
+  return t;
+}
+
+static int64_t max_coarse_entries(const int32_t* seg_row, int nseg) {
+  int64_t t = 0;
+  for (int s = 0; s < nseg; ++s) {
+    const int64_t c = std::min<int64_t>(seg_cap(seg_row[s + 1] - seg_row[s]), kCoarseMaxDim);
+    t += c * c;
+  }
+  return t;
+}
+
+size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg) {
+  const int64_t na = two_level_max_aggs(seg_row, nseg);
+  const int64_t ne = max_coarse_entries(seg_row, nseg);
+  return a256(4 * (size_t)n) * 2 + a256(4 * (size_t)(na + 1)) + a256(4 * (size_t)na) +
+         a256(4 * (size_t)(nseg + 1)) + a256(8 * (size_t)(nseg + 1)) + a256(4 * (size_t)ne) +
+         a256(8 * (size_t)ne) + a256(4 * (size_t)nseg) + 1024;
+}
+
+// ---- host aggregation -------------------------------------------------------
+// Labels rows [r0, r1) with local aggregate ids 0..nc-1 (lab: global array).
+static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, const int32_t* indices,
+                             int32_t* lab) {
+  const int32_t len = r1 - r0;
+  if (len <= 0) return 0;
+  for (int32_t v = r0; v < r1; ++v) lab[v] = -1;
+  std::vector<int32_t> queue;
+  queue.reserve(kAggTarget);
+  int32_t id = 0;
+  for (int32_t v = r0; v < r1; ++v) {
+    if (lab[v] >= 0) continue;
+    queue.clear();
+    queue.push_back(v);
+    lab[v] = id;
+    int cnt = 1;
+    for (size_t qi = 0; qi < queue.size() && cnt < kAggTarget; ++qi) {
+      const int32_t u = queue[qi];
+      for (int32_t k = indptr[u]; k < indptr[u + 1] && cnt < kAggTarget; ++k) {
+        const int32_t w = indices[k];
+        if (w < r0 || w >= r1 || lab[w] >= 0) continue;
+        lab[w] = id;
+        queue.push_back(w);
+        ++cnt;
+      }
+    }
+    ++id;
+  }
+  // merge aggregates below kAggTarget / 4 rows into the neighbour aggregate
+  // with the most connecting entries (ties: the smaller id)
+  std::vector<std::vector<int32_t>> members(id);
+  for (int32_t v = r0; v < r1; ++v) members[lab[v]].push_back(v);
+  std::vector<int32_t> parent(id);
+  for (int32_t a = 0; a < id; ++a) parent[a] = a;
+  auto find = [&](int32_t a) {
+    while (parent[a] != a) a = parent[a] = parent[parent[a]];
+    return a;
+  };
+  std::vector<int32_t> conn_ids;
+  std::vector<int32_t> conn_cnt;
+  for (int32_t a = 0; a < id; ++a) {
+    if (parent[a] != a || (int)members[a].size() >= kAggTarget / 4) continue;
+    conn_ids.clear();
+    conn_cnt.clear();
+    for (int32_t u : members[a]) {
+      for (int32_t k = indptr[u]; k < indptr[u + 1]; ++k) {
+        const int32_t w = indices[k];
+        if (w < r0 || w >= r1) continue;
+        const int32_t b = find(lab[w]);
+        if (b == a) continue;
+        size_t t = 0;
+        while (t < conn_ids.size() && conn_ids[t] != b) ++t;
+        if (t == conn_ids.size()) {
+          conn_ids.push_back(b);
+          conn_cnt.push_back(0);
+        }
+        ++conn_cnt[t];
+      }
+    }
+    if (conn_ids.empty()) continue;  // an isolated component stays on its own
+    size_t best = 0;
+    for (size_t t = 1; t < conn_ids.size(); ++t)
+      if (conn_cnt[t] > conn_cnt[best] || (conn_cnt[t] == conn_cnt[best] && conn_ids[t] < conn_ids[best]))
+        best = t;
+    const int32_t b = conn_ids[best];
+    parent[a] = b;
+    members[b].insert(members[b].end(), members[a].begin(), members[a].end());
+    members[a].clear();
+  }
+  // compact: ids in order of each aggregate's first row
+  std::vector<int32_t> remap(id, -1);
+  int32_t nc = 0;
+  for (int32_t v = r0; v < r1; ++v) {
+    const int32_t a = find(lab[v]);
+    if (remap[a] < 0) remap[a] = nc++;
+    lab[v] = remap[a];
+  }
+  if (nc > std::min<int64_t>(seg_cap(len), kCoarseMaxDim)) {
+    for (int32_t v = r0; v < r1; ++v) lab[v] = -1;
+    return 0;
+  }
+  return nc;
+}
+
+// ---- device kernels ---------------------------------------------------------
+// Row g - seg_agg[s] of segment s's Galerkin matrix: sum of K over the
+// aggregate's rows, accumulated per coarse column in row / CSR order.
+__global__ void coarse_galerkin_kernel(int nagg, const int32_t* __restrict__ agg, const int32_t* __restrict__ agg_ptr,
+                                       const int32_t* __restrict__ agg_row, const int32_t* __restrict__ agg_sid,
+                                       const int32_t* __restrict__ seg_agg, const int64_t* __restrict__ off,
+                                       const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                       const double* __restrict__ k64, double* __restrict__ kc) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nagg) return;
+  const int s = agg_sid[g];
+  const int base = seg_agg[s];
+  const int nc = seg_agg[s + 1] - base;
+  double* row = kc + off[s] + (int64_t)(g - base) * nc;
+  for (int32_t m = agg_ptr[g]; m < agg_ptr[g + 1]; ++m) {
+    const int32_t i = agg_row[m];
+    for (int32_t k = indptr[i]; k < indptr[i + 1]; ++k) {
+      const int32_t b = agg[indices[k]] - base;
+      if (b >= 0 && b < nc) row[b] += k64[k];
+    }
+  }
+}
+
+constexpr int kInvThreads = 512;
+
+// In-place inverse of one SPD block A (nc x nc, row-major, FP64) per CTA:
+// A = L L' (lower triangle), B = L^-1 kept transposed in the strict upper
+// triangle with its diagonal in shared memory, then A^-1 = B'B written to
+// `out` in FP32.  A non-positive pivot leaves the segment's block zero (no
+// coarse correction: the preconditioner falls back to Jacobi there).
+__global__ void __launch_bounds__(kInvThreads) coarse_inverse_kernel(const int32_t* __restrict__ seg_agg,
+                                                                     const int64_t* __restrict__ off,
+                                                                     double* __restrict__ kc,
+                                                                     float* __restrict__ out,
+                                                                     int* __restrict__ failed) {
+  __shared__ double col[kCoarseMaxDim];
+  __shared__ double diagb[kCoarseMaxDim];
+  __shared__ int ok;
+  const int s = blockIdx.x;
+  const int nc = seg_agg[s + 1] - seg_agg[s];
+  if (nc <= 0) return;
+  double* A = kc + off[s];
+  float* O = out + off[s];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = kInvThreads / 32;
+  if (tid == 0) ok = 1;
+  __syncthreads();
+  // Cholesky, right-looking; the pivot column is staged in shared memory
+  for (int k = 0; k < nc; ++k) {
+    if (tid == 0) {
+      const double piv = A[(int64_t)k * nc + k];
+      if (!(piv > 0.0) || !isfinite(piv)) ok = 0;
+      const double d = ok ? sqrt(piv) : 1.0;
+      A[(int64_t)k * nc + k] = d;
+      col[k] = d;
+    }
+    __syncthreads();
+    if (!ok) break;
+    const double d = col[k];
+    for (int i = k + 1 + tid; i < nc; i += kInvThreads) {
+      const double l = A[(int64_t)i * nc + k] / d;
+      A[(int64_t)i * nc + k] = l;
+      col[i] = l;
+    }
+    __syncthreads();
+    for (int i = k + 1 + warp; i < nc; i += nwarp) {
+      const double ci = col[i];
+      double* Ai = A + (int64_t)i * nc;
+      for (int j = k + 1 + lane; j <= i; j += 32) Ai[j] -= ci * col[j];
+    }
+    __syncthreads();
+  }
+  if (!ok) {
+    for (int64_t t = tid; t < (int64_t)nc * nc; t += kInvThreads) O[t] = 0.0f;
+    if (tid == 0) failed[s] = 1;
+    return;
+  }
+  // B = L^-1: row c of U (= column c of B) lives in A[c][c+1..nc), B[c][c] in diagb
+  for (int c = tid; c < nc; c += kInvThreads) diagb[c] = 1.0;
+  for (int c = warp; c < nc; c += nwarp)
+    for (int i = c + 1 + lane; i < nc; i += 32) A[(int64_t)c * nc + i] = 0.0;
+  __syncthreads();
+  for (int j = 0; j < nc; ++j) {
+    // stage column j of L and scale row j of B by 1 / L[j][j]
+    for (int i = j + tid; i < nc; i += kInvThreads) col[i] = A[(int64_t)i * nc + j];
+    __syncthreads();
+    const double inv = 1.0 / col[j];
+    for (int c = tid; c < j; c += kInvThreads) A[(int64_t)c * nc + j] *= inv;
+    if (tid == 0) diagb[j] *= inv;
+    __syncthreads();
+    // B[i][c] -= L[i][j] B[j][c] for i > j, c <= j
+    for (int c = warp; c <= j; c += nwarp) {
+      const double bjc = (c < j) ? A[(int64_t)c * nc + j] : diagb[j];
+      double* Uc = A + (int64_t)c * nc;
+      for (int i = j + 1 + lane; i < nc; i += 32) Uc[i] -= col[i] * bjc;
+    }
+    __syncthreads();
+  }
+  // A^-1 [a][b] = sum_{i >= max(a,b)} B[i][a] B[i][b]   (rows a, b of U);
+  // one warp per row a, pairs b >= a
+  for (int a = warp; a < nc; a += nwarp) {
+    const double* Ua = A + (int64_t)a * nc;
+    for (int b = a; b < nc; ++b) {
+      const double* Ub = A + (int64_t)b * nc;
+      double acc = 0.0;
+      for (int i = b + lane; i < nc; i += 32) {
+        const double ua = (i == a) ? diagb[a] : Ua[i];
+        const double ub = (i == b) ? diagb[b] : Ub[i];
+        acc += ua * ub;
+      }
+      acc = warp_sum(acc);
+      if (lane == 0) {
+        O[(int64_t)a * nc + b] = (float)acc;
+        O[(int64_t)b * nc + a] = (float)acc;
+      }
+    }
+  }
+}
+
+int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64,
+                    const int32_t* seg_row, int nseg, void* mem, size_t bytes, PcgPrecondDesc<float>* pc,
+                    cudaStream_t stream) {
+  if (bytes < two_level_bytes(n, seg_row, nseg)) return LAPY_ERR_WORKSPACE;
+  // pattern to the host
+  std::vector<int32_t> hptr(n + 1);
+  LAPY_CUDA_TRY(cudaMemcpyAsync(hptr.data(), indptr, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, stream));
+  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+  const int64_t nnz = hptr[n];
+  std::vector<int32_t> hidx(nnz);
+  LAPY_CUDA_TRY(cudaMemcpyAsync(hidx.data(), indices, 4 * (size_t)nnz, cudaMemcpyDeviceToHost, stream));
+  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+
+  std::vector<int32_t> lab(n, -1), nc(nseg, 0);
+  const int nthr = std::max(1, std::min<int>(nseg, std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+  {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthr; ++t)
+      pool.emplace_back([&, t]() {
+        for (int s = t; s < nseg; s += nthr)
+          nc[s] = aggregate_segment(seg_row[s], seg_row[s + 1], hptr.data(), hidx.data(), lab.data());
+      });
+    for (auto& th : pool) th.join();
+  }
+  std::vector<int32_t> seg_agg(nseg + 1, 0);
+  std::vector<int64_t> off(nseg + 1, 0);
+  for (int s = 0; s < nseg; ++s) {
+    seg_agg[s + 1] = seg_agg[s] + nc[s];
+    off[s + 1] = off[s] + (int64_t)nc[s] * nc[s];
+  }
+  const int nagg = seg_agg[nseg];
+  std::vector<int32_t> agg(n, -1), agg_sid(nagg), agg_ptr(nagg + 1, 0), agg_row;
+  for (int s = 0; s < nseg; ++s)
+    for (int32_t v = seg_row[s]; v < seg_row[s + 1]; ++v)
+      if (lab[v] >= 0) agg[v] = seg_agg[s] + lab[v];
+  for (int s = 0; s < nseg; ++s)
+    for (int g = seg_agg[s]; g < seg_agg[s + 1]; ++g) agg_sid[g] = s;
+  for (int64_t v = 0; v < n; ++v)
+    if (agg[v] >= 0) ++agg_ptr[agg[v] + 1];
+  for (int g = 0; g < nagg; ++g) agg_ptr[g + 1] += agg_ptr[g];
+  agg_row.resize(agg_ptr[nagg]);
+  {
+    std::vector<int32_t> fill(agg_ptr.begin(), agg_ptr.end() - 1);
+    for (int64_t v = 0; v < n; ++v)
+      if (agg[v] >= 0) agg_row[fill[agg[v]]++] = (int32_t)v;
+  }
+
+  // device layout
+  char* w = (char*)(((uintptr_t)mem + 255) & ~uintptr_t(255));
+  const int64_t na_max = two_level_max_aggs(seg_row, nseg);
+  const int64_t ne_max = max_coarse_entries(seg_row, nseg);
+  if (nagg > na_max || off[nseg] > ne_max) {
+    lapy_set_last_message("two-level: coarse space exceeds its bound");
+    return LAPY_ERR_WORKSPACE;
+  }
+  int32_t* d_agg = (int32_t*)w; w += a256(4 * (size_t)n);
+  int32_t* d_row = (int32_t*)w; w += a256(4 * (size_t)n);
+  int32_t* d_ptr = (int32_t*)w; w += a256(4 * (size_t)(na_max + 1));
+  int32_t* d_sid = (int32_t*)w; w += a256(4 * (size_t)na_max);
+  int32_t* d_seg = (int32_t*)w; w += a256(4 * (size_t)(nseg + 1));
+  int64_t* d_off = (int64_t*)w; w += a256(8 * (size_t)(nseg + 1));
+  float* d_kinv = (float*)w; w += a256(4 * (size_t)ne_max);
+  double* d_kc = (double*)w; w += a256(8 * (size_t)ne_max);
+  int* d_fail = (int*)w;
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_agg, agg.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
+  if (!agg_row.empty())
+    LAPY_CUDA_TRY(cudaMemcpyAsync(d_row, agg_row.data(), 4 * agg_row.size(), cudaMemcpyHostToDevice, stream));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_ptr, agg_ptr.data(), 4 * agg_ptr.size(), cudaMemcpyHostToDevice, stream));
+  if (nagg > 0)
+    LAPY_CUDA_TRY(cudaMemcpyAsync(d_sid, agg_sid.data(), 4 * (size_t)nagg, cudaMemcpyHostToDevice, stream));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_seg, seg_agg.data(), 4 * seg_agg.size(), cudaMemcpyHostToDevice, stream));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_off, off.data(), 8 * off.size(), cudaMemcpyHostToDevice, stream));
+  if (off[nseg] > 0) LAPY_CUDA_TRY(cudaMemsetAsync(d_kc, 0, 8 * (size_t)off[nseg], stream));
+  LAPY_CUDA_TRY(cudaMemsetAsync(d_fail, 0, 4 * (size_t)nseg, stream));
+  if (nagg > 0) {
+    coarse_galerkin_kernel<<<lapy_ceil_div(nagg, 128), 128, 0, stream>>>(nagg, d_agg, d_ptr, d_row, d_sid, d_seg, d_off,
+                                                                         indptr, indices, k64, d_kc);
+    LAPY_TRY(lapy_check_launch("coarse_galerkin_kernel"));
+    coarse_inverse_kernel<<<nseg, kInvThreads, 0, stream>>>(d_seg, d_off, d_kc, d_kinv, d_fail);
+    LAPY_TRY(lapy_check_launch("coarse_inverse_kernel"));
+  }
+  // the host vectors are pageable: the copies complete before they go away
+  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+  pc->kind = kPrecTwoLevel;
+  pc->nagg = nagg;
+  pc->agg = d_agg;
+  pc->agg_ptr = d_ptr;
+  pc->agg_row = d_row;
+  pc->agg_sid = d_sid;
+  pc->seg_agg = d_seg;
+  pc->kinv_off = d_off;
+  pc->kinv = d_kinv;
+  return LAPY_OK;
+}
+
+}  // namespace lapy

@@ -22,6 +22,7 @@
 #include "blas.cuh"
 #include "dense.cuh"
 #include "solve.cuh"
+#include "coarse.cuh"
 #include "spmv.cuh"
 
 namespace lapy {
@@ -352,6 +353,8 @@ __global__ void rr_finish_kernel(int keff, int k, const double* __restrict__ Lm,
 struct EigPlan {
   int64_t n, nnz;
   int nseg, p, k, keff, mb, lda;
+  int precond = kPrecJacobi;  // inner PCG: Jacobi or two-level
+  int64_t nagg_max = 0;
   ChunkTable ct;   // PCG chunks
   ChunkTable gt;   // GEMM chunks (larger)
 };
@@ -362,6 +365,7 @@ struct EigPtrs {
   double* basis; double* Y; double* W; double* MW;
   void* ir_ws; size_t ir_bytes;
   void* sell_mem; size_t sell_bytes;
+  void* tl_mem; size_t tl_bytes;
   double* partial;
   double* H; double* Hsum; double* G; double* R1; double* R2; double* Bm;
   double* T; double* Tc; double* theta; double* S; double* eigw;
@@ -372,8 +376,10 @@ struct EigPtrs {
 };
 
 static void plan_eig(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, int k, int p, int max_vectors,
-                     EigPlan* P) {
+                     int precond, EigPlan* P) {
   P->n = n; P->nnz = nnz; P->nseg = nseg; P->p = p; P->k = k;
+  P->precond = precond;
+  P->nagg_max = precond == kPrecTwoLevel ? two_level_max_aggs(seg_row, nseg) : 0;
   P->keff = k + p;
   P->mb = std::max((max_vectors + p - 1) / p, (P->keff + 2 * p + p - 1) / p + 1);
   P->lda = P->mb * p;
@@ -403,8 +409,10 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.Y = (double*)take(8 * n * p);
   e.W = (double*)take(8 * n * p);
   e.MW = (double*)take(8 * n * p);
-  e.ir_bytes = ir_workspace_bytes(n, p, P.ct, 1, kPrecJacobi);
+  e.ir_bytes = ir_workspace_bytes(n, p, P.ct, 1, P.precond, P.nagg_max);
   e.ir_ws = take(e.ir_bytes);
+  e.tl_bytes = P.precond == kPrecTwoLevel ? two_level_bytes(n, P.ct.h_seg_row.data(), ns) : 0;
+  e.tl_mem = take(e.tl_bytes);
   e.sell_bytes = sell_bytes_bound(nnz, P.ct, sizeof(float));
   e.sell_mem = take(e.sell_bytes);
   const size_t part_elems = (size_t)P.gt.nchunk * std::max((size_t)lda * p, (size_t)keff * keff);
@@ -530,6 +538,8 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     LAPY_TRY(build_sell<float>(n, indptr, indices, e.k32, P.ct, e.sell_mem, e.sell_bytes, &K.sell32, &fits, st));
     if (!fits) K.sell32 = SellMatrix<float>();
   }
+  if (P.precond == kPrecTwoLevel)
+    LAPY_TRY(build_two_level(n, indptr, indices, e.k64, P.ct.h_seg_row.data(), ns, e.tl_mem, e.tl_bytes, &K.pc32, st));
 
   std::vector<int32_t> hact(ns, 1), hnsize(ns, 0);
   LAPY_CUDA_TRY(cudaMemcpyAsync(e.active, hact.data(), 4 * ns, cudaMemcpyHostToDevice, st));
@@ -668,11 +678,14 @@ using namespace lapy;
 
 static int eig_block_ok(int p) { return p == 1 || p == 2 || p == 4 || p == 8 || p == 16; }
 
+static int eig_precond_ok(int pc) { return pc == kPrecJacobi || pc == kPrecTwoLevel; }
+
 extern "C" size_t lapy_eigs_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, int k,
-                                            int block, int max_vectors) {
-  if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || k <= 0 || !eig_block_ok(block)) return 0;
+                                            int block, int max_vectors, int precond) {
+  if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || k <= 0 || !eig_block_ok(block) || !eig_precond_ok(precond))
+    return 0;
   EigPlan P;
-  plan_eig(n, nnz, nseg, seg_row, k, block, max_vectors, &P);
+  plan_eig(n, nnz, nseg, seg_row, k, block, max_vectors, precond, &P);
   return layout_eig(P, nullptr, nullptr);
 }
 
@@ -680,11 +693,12 @@ extern "C" int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const in
                                       const double* a_vals, const double* m_vals, int m_is_diag, int64_t nnz,
                                       int nseg, const int32_t* seg_row, double sigma, int k, int block,
                                       int max_vectors, double tol, double inner_rtol, int inner_maxiter,
-                                      uint64_t seed, double* evals, double* evecs, int32_t* status_out,
+                                      int precond, uint64_t seed, double* evals, double* evecs, int32_t* status_out,
                                       int32_t* nbasis_out, int64_t* inner_iters_out, void* ws, size_t ws_bytes,
                                       void* stream) {
   if (n <= 0 || !indptr || !indices || !a_vals || !m_vals || nnz <= 0 || nseg <= 0 || !seg_row || k <= 0 ||
-      !eig_block_ok(block) || !evals || !evecs || !ws || !(tol > 0) || !(inner_rtol > 0) || inner_maxiter <= 0) {
+      !eig_block_ok(block) || !evals || !evecs || !ws || !(tol > 0) || !(inner_rtol > 0) || inner_maxiter <= 0 ||
+      !eig_precond_ok(precond)) {
     lapy_set_last_message("eigs_shift_invert: invalid arguments");
     return LAPY_ERR_INVALID;
   }
@@ -701,7 +715,7 @@ extern "C" int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const in
     }
   }
   EigPlan P;
-  plan_eig(n, nnz, nseg, seg_row, k, block, max_vectors, &P);
+  plan_eig(n, nnz, nseg, seg_row, k, block, max_vectors, precond, &P);
   if (ws_bytes < layout_eig(P, nullptr, nullptr)) return LAPY_ERR_WORKSPACE;
   EigPtrs e;
   layout_eig(P, (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255)), &e);

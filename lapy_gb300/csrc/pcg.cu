@@ -153,6 +153,9 @@ struct PcgArgs {
   V* Z;
   V* T;
   S* part;            // [3][npiece][NP]  pq, rz, rr
+  S* rc;              // [nagg][NP] restricted residual W'r   (two-level)
+  S* yc;              // [nagg][NP] coarse solution (W'KW)^-1 W'r
+  S* csl;             // [nagg][NP] rc .* yc (coarse part of r'z)
   S* rz;              // [2][nseg][NP]
   S* bb;              // [nseg][NP]
   int32_t* state;     // [2][nseg][NP]
@@ -163,6 +166,19 @@ struct PcgArgs {
   S rtol2;
   int maxiter;
   GridBarrier bar;
+  // reliable updates (RU variant): FP64 right-hand side, solution and matrix;
+  // X above is then the FP32 correction accumulated since the last update
+  const double* B64;   // n x NP
+  double* X64;         // n x NP
+  const double* K64;   // FP64 values on indptr / indices
+  double* part64;      // [npiece][NP]  partial ||b - K x||^2
+  S* rref;             // [nseg][NP]    squared residual at the last update
+  int32_t* ru_col;     // [2][nseg][NP] update requests (by parity)
+  unsigned* ru_flag;   // [2]           any request (by parity)
+  unsigned* n_updates; // [1]           update sweeps performed
+  double rtol2_64;
+  S delta2;
+  int ru_every;
 };
 
 // NP consecutive values of row `row` (vectorised: rows are NP * sizeof(V)
@@ -316,6 +332,89 @@ __device__ __forceinline__ void sell_unit_spmm(const SellMatrix<V>& M, const V* 
   }
 }
 
+// Two-level preconditioner, restriction: rc = W' R for the aggregates of
+// segments with an active column (all == true: every aggregate).
+template <typename V, int NP>
+__device__ __forceinline__ void coarse_restrict(const PcgArgs<V>& a, const int32_t* st, bool all, int gw, int nw) {
+  using S = ScalarOf<V>;
+  const int lane = threadIdx.x & 31;
+  for (int g = gw; g < a.pc.nagg; g += nw) {
+    const int s = a.pc.agg_sid[g];
+    if (!all) {
+      bool act = false;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) act |= st[s * NP + q] == kActive;
+      if (!act) continue;
+    }
+    S acc[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) acc[q] = S(0);
+    for (int32_t m = a.pc.agg_ptr[g] + lane; m < a.pc.agg_ptr[g + 1]; m += 32) {
+      V r[NP];
+      load_row<V, NP>(a.R, a.pc.agg_row[m], r);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] += (S)r[q];
+    }
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const S v = warp_sum(acc[q]);
+      if (lane == q) a.rc[(int64_t)g * NP + q] = v;
+    }
+  }
+}
+
+// Two-level preconditioner, coarse solve: yc = (W'KW)^-1 rc per segment (one
+// warp per coarse row) and csl = rc .* yc.
+template <typename V, int NP>
+__device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t* st, bool all, int gw, int nw) {
+  using S = ScalarOf<V>;
+  const int lane = threadIdx.x & 31;
+  for (int g = gw; g < a.pc.nagg; g += nw) {
+    const int s = a.pc.agg_sid[g];
+    if (!all) {
+      bool act = false;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) act |= st[s * NP + q] == kActive;
+      if (!act) continue;
+    }
+    const int base = a.pc.seg_agg[s];
+    const int nc = a.pc.seg_agg[s + 1] - base;
+    const float* __restrict__ kr = a.pc.kinv + a.pc.kinv_off[s] + (int64_t)(g - base) * nc;
+    const S* __restrict__ rcs = a.rc + (int64_t)base * NP;
+    S acc[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) acc[q] = S(0);
+    for (int j = lane; j < nc; j += 32) {
+      const S kv = (S)__ldg(kr + j);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] += kv * rcs[(int64_t)j * NP + q];
+    }
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const S y = warp_sum(acc[q]);
+      if (lane == q) {
+        a.yc[(int64_t)g * NP + q] = y;
+        a.csl[(int64_t)g * NP + q] = y * a.rc[(int64_t)g * NP + q];
+      }
+    }
+  }
+}
+
+// z = dinv .* r (+ the coarse correction W yc for the two-level preconditioner)
+template <typename V, int NP, int PC>
+__device__ __forceinline__ void apply_diag_coarse(const PcgArgs<V>& a, int row, const V (&r)[NP], V (&z)[NP]) {
+  const V d = a.pc.dinv[row];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) z[q] = d * r[q];
+  if constexpr (PC == kPrecTwoLevel) {
+    const int g = a.pc.agg[row];
+    if (g >= 0) {
+#pragma unroll
+      for (int q = 0; q < NP; ++q) z[q] += (V)a.yc[(int64_t)g * NP + q];
+    }
+  }
+}
+
 // Loop over this warp's pieces: s = segment, [u0, u1) = units of the piece.
 #define FOR_MY_PIECES(a, ...)                                                               \
   for (int vw = gw; vw < (a).nvw; vw += nw) {                                                \
@@ -327,7 +426,7 @@ __device__ __forceinline__ void sell_unit_spmm(const SellMatrix<V>& M, const V* 
     }                                                                                        \
   }
 
-template <typename V, int NP, int PC>
+template <typename V, int NP, int PC, bool RU>
 __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   using S = ScalarOf<V>;
   __shared__ V sval_all[kWarps * kStageWarp];
@@ -339,6 +438,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   S* part_pq = a.part;
   S* part_rz = a.part + (int64_t)a.npiece * NP;
   S* part_rr = a.part + 2 * (int64_t)a.npiece * NP;
+  constexpr bool kDiagPC = PC == kPrecJacobi || PC == kPrecTwoLevel;  // z = dinv .* r (+ coarse term)
 
   // ---- phase 0: X = 0, R = B, P = M^-1 R (Jacobi); partial b'b and r'z
   FOR_MY_PIECES(a, {
@@ -349,24 +449,38 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
       const int row = a.unit_row[u] + lane;
       if (row < a.unit_row[u + 1]) {
         V b[NP], z[NP], zero[NP];
-        load_row<V, NP>(a.B, row, b);
+        if constexpr (RU) {
+          double b64[NP], z64[NP];
+          load_row<double, NP>(a.B64, row, b64);
+#pragma unroll
+          for (int q = 0; q < NP; ++q) { b[q] = (V)b64[q]; z64[q] = 0.0; }
+          store_row<double, NP>(a.X64, row, z64);
+        } else {
+          load_row<V, NP>(a.B, row, b);
+        }
 #pragma unroll
         for (int q = 0; q < NP; ++q) zero[q] = V(0);
         store_row<V, NP>(a.X, row, zero);
         store_row<V, NP>(a.R, row, b);
-        if (PC == kPrecJacobi) {
+        if (kDiagPC) {
           const V d = a.pc.dinv[row];
 #pragma unroll
           for (int q = 0; q < NP; ++q) { z[q] = d * b[q]; rz[q] += b[q] * z[q]; }
-          store_row<V, NP>(a.P, row, z);
+          if (PC == kPrecJacobi) store_row<V, NP>(a.P, row, z);
         }
 #pragma unroll
         for (int q = 0; q < NP; ++q) bb[q] += b[q] * b[q];
       }
     }
     warp_store_partials<NP>(bb, part_rr + (int64_t)p * NP);
-    if (PC == kPrecJacobi) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
+    if (kDiagPC) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
   })
+  if constexpr (PC == kPrecTwoLevel) {
+    if (!grid_sync(a.bar)) return;
+    coarse_restrict<V, NP>(a, nullptr, true, gw, nw);
+    if (!grid_sync(a.bar)) return;
+    coarse_solve<V, NP>(a, nullptr, true, gw, nw);
+  }
   if (PC == kPrecFactored) {
     S dummy[NP];
     if (!grid_sync(a.bar)) return;
@@ -389,10 +503,27 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   if (!grid_sync(a.bar)) return;
   // ---- segment initialisation (the warp holding a segment's first piece publishes)
   FOR_MY_PIECES(a, {
+    if constexpr (PC == kPrecTwoLevel) {
+      for (int u = u0; u < u1; ++u) {
+        const int row = a.unit_row[u] + lane;
+        if (row < a.unit_row[u + 1]) {
+          V r[NP], z[NP];
+          load_row<V, NP>(a.R, row, r);
+          apply_diag_coarse<V, NP, PC>(a, row, r, z);
+          store_row<V, NP>(a.P, row, z);
+        }
+      }
+    }
     if (a.seg_piece[s] == p) {
       S bb[NP], rz[NP];
       seg_totals<NP>(part_rr, a.seg_piece[s], a.seg_piece[s + 1], bb);
       seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rz);
+      if constexpr (PC == kPrecTwoLevel) {
+        S c[NP];
+        seg_totals<NP>(a.csl, a.pc.seg_agg[s], a.pc.seg_agg[s + 1], c);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) rz[q] += c[q];
+      }
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         if (lane == q) {
@@ -403,6 +534,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
           else st = kActive;
           a.bb[s * NP + q] = bb[q];
           a.rz[s * NP + q] = rz[q];
+          if (RU) a.rref[s * NP + q] = bb[q];
           a.state[s * NP + q] = st;
           if (st == kActive) atomicAdd(&a.active[0], 1u);
         }
@@ -421,10 +553,131 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
     const unsigned nact = *((volatile unsigned*)&a.active[par]);
     if (nact == 0 || it >= a.maxiter) break;
 
+    // ---- reliable update of the columns flagged in the previous phase C:
+    // X64 += X (FP32 correction), X = 0; then R = b - K64 X64 in FP64
+    bool ru_now = false;
+    const int32_t* ru_req = nullptr;
+    if constexpr (RU) {
+      ru_req = a.ru_col + par * (int64_t)a.nseg * NP;
+      ru_now = *((volatile unsigned*)&a.ru_flag[par]) != 0u;
+      if (ru_now) {
+        FOR_MY_PIECES(a, {
+          bool fl[NP];
+          bool anyf = false;
+#pragma unroll
+          for (int q = 0; q < NP; ++q) { fl[q] = ru_req[s * NP + q] != 0; anyf |= fl[q]; }
+          if (anyf) {
+            for (int u = u0; u < u1; ++u) {
+              const int row = a.unit_row[u] + lane;
+              if (row < a.unit_row[u + 1]) {
+                V x[NP];
+                double x64[NP];
+                load_row<V, NP>(a.X, row, x);
+                load_row<double, NP>(a.X64, row, x64);
+#pragma unroll
+                for (int q = 0; q < NP; ++q)
+                  if (fl[q]) { x64[q] += (double)x[q]; x[q] = V(0); }
+                store_row<double, NP>(a.X64, row, x64);
+                store_row<V, NP>(a.X, row, x);
+              }
+            }
+          }
+        })
+        if (!grid_sync(a.bar)) return;
+        FOR_MY_PIECES(a, {
+          bool fl[NP];
+          bool anyf = false;
+#pragma unroll
+          for (int q = 0; q < NP; ++q) { fl[q] = ru_req[s * NP + q] != 0; anyf |= fl[q]; }
+          double rr[NP];
+          S rz[NP];
+#pragma unroll
+          for (int q = 0; q < NP; ++q) { rr[q] = 0.0; rz[q] = S(0); }
+          if (anyf) {
+            for (int u = u0; u < u1; ++u) {
+              const int row = a.unit_row[u] + lane;
+              if (row < a.unit_row[u + 1]) {
+                double acc[NP], b64[NP];
+#pragma unroll
+                for (int q = 0; q < NP; ++q) acc[q] = 0.0;
+                const int32_t kb = a.indptr[row], ke = a.indptr[row + 1];
+                for (int32_t k = kb; k < ke; ++k) {
+                  const double v = __ldg(a.K64 + k);
+                  double xr[NP];
+                  load_row<double, NP>(a.X64, __ldg(a.indices + k), xr);
+#pragma unroll
+                  for (int q = 0; q < NP; ++q) acc[q] = fma(v, xr[q], acc[q]);
+                }
+                load_row<double, NP>(a.B64, row, b64);
+                V r[NP];
+                load_row<V, NP>(a.R, row, r);
+                const V d = a.pc.dinv[row];
+#pragma unroll
+                for (int q = 0; q < NP; ++q) {
+                  if (fl[q]) {
+                    const double r64 = b64[q] - acc[q];
+                    rr[q] += r64 * r64;
+                    r[q] = (V)r64;
+                    rz[q] += r[q] * (d * r[q]);
+                  }
+                }
+                store_row<V, NP>(a.R, row, r);
+              }
+            }
+          }
+          warp_store_partials<NP>(rr, a.part64 + (int64_t)p * NP);
+          warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
+        })
+        if (!grid_sync(a.bar)) return;
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.n_updates, 1u);
+      }
+    }
+
     // ---- phase A: Q = K P, partial p'q
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.active[par ^ 1] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.active[par ^ 1] = 0u;
+      if (RU) a.ru_flag[par ^ 1] = 0u;
+    }
     FOR_MY_PIECES(a, {
-      const bool any = __any_sync(0xffffffffu, lane < NP && st_cur[s * NP + (lane % NP)] == kActive);
+      bool colact[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) colact[q] = st_cur[s * NP + q] == kActive;
+      if constexpr (RU) {
+        const bool first = a.seg_piece[s] == p;
+        if (first && lane < NP) a.ru_col[(par ^ 1) * (int64_t)a.nseg * NP + s * NP + lane] = 0;
+        bool fl[NP];
+        bool anyf = false;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) { fl[q] = ru_now && ru_req[s * NP + q] != 0; anyf |= fl[q]; }
+        if (anyf) {
+          // the true residual decides convergence; otherwise CG continues with
+          // the same direction P and the new r'z
+          double rr64[NP];
+          S rzt[NP];
+          seg_totals<NP>(a.part64, a.seg_piece[s], a.seg_piece[s + 1], rr64);
+          seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rzt);
+#pragma unroll
+          for (int q = 0; q < NP; ++q) {
+            if (!(fl[q] && colact[q])) continue;
+            int32_t st = kActive;
+            if (!isfinite(rr64[q]) || !isfinite(rzt[q])) st = LAPY_ERR_NAN;
+            else if (rr64[q] <= a.rtol2_64 * (double)a.bb[s * NP + q]) st = it > 0 ? it : 1;
+            else if (!(rzt[q] > S(0))) st = LAPY_ERR_BREAKDOWN;
+            colact[q] = st == kActive;
+            if (first && lane == q) {
+              const_cast<int32_t*>(st_cur)[s * NP + q] = st;
+              if (st == kActive) {
+                const_cast<S*>(rz_cur)[s * NP + q] = rzt[q];
+                a.rref[s * NP + q] = (S)rr64[q];
+              }
+            }
+          }
+        }
+      }
+      bool mine = false;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) mine |= (lane == q) && colact[q];
+      const bool any = __any_sync(0xffffffffu, mine);
       S acc[NP];
 #pragma unroll
       for (int q = 0; q < NP; ++q) acc[q] = S(0);
@@ -472,7 +725,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
             load_row<V, NP>(a.P, row, pv);
             load_row<V, NP>(a.Q, row, qv);
             load_row<V, NP>(a.R, row, r);
-            const V d = (PC == kPrecJacobi) ? a.pc.dinv[row] : V(0);
+            const V d = kDiagPC ? a.pc.dinv[row] : V(0);
 #pragma unroll
             for (int q = 0; q < NP; ++q) {
               if (act[q]) {
@@ -480,7 +733,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
                 r[q] = r[q] - alpha[q] * qv[q];
               }
               rr[q] += r[q] * r[q];
-              if (PC == kPrecJacobi) rz[q] += r[q] * (d * r[q]);
+              if (kDiagPC) rz[q] += r[q] * (d * r[q]);
             }
             store_row<V, NP>(a.X, row, x);
             store_row<V, NP>(a.R, row, r);
@@ -488,9 +741,17 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
         }
       }
       warp_store_partials<NP>(rr, part_rr + (int64_t)p * NP);
-      if (PC == kPrecJacobi) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
+      if (kDiagPC) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
     })
     if (!grid_sync(a.bar)) return;
+
+    if constexpr (PC == kPrecTwoLevel) {
+      // ---- phases R, G: coarse correction of the new residual
+      coarse_restrict<V, NP>(a, st_cur, false, gw, nw);
+      if (!grid_sync(a.bar)) return;
+      coarse_solve<V, NP>(a, st_cur, false, gw, nw);
+      if (!grid_sync(a.bar)) return;
+    }
 
     if (PC == kPrecFactored) {
       // ---- phase B2: T = G R ; phase B3: Z = Gt T, partial r'z
@@ -519,27 +780,45 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
       seg_totals<NP>(part_pq, a.seg_piece[s], a.seg_piece[s + 1], pq);
       seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rzn);
       seg_totals<NP>(part_rr, a.seg_piece[s], a.seg_piece[s + 1], rr);
+      if constexpr (PC == kPrecTwoLevel) {
+        S c[NP];
+        seg_totals<NP>(a.csl, a.pc.seg_agg[s], a.pc.seg_agg[s + 1], c);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) rzn[q] += c[q];
+      }
       V beta[NP];
       bool act[NP];
       bool any = false;
       const bool first = a.seg_piece[s] == p;
+      const bool ru_slot = RU && ((it + 1) % a.ru_every == 0);
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         const int32_t st0 = st_cur[s * NP + q];
         int32_t st = st0;
+        bool req = false;
         if (st0 == kActive) {
           if (!(pq[q] > S(0)) || !isfinite(pq[q])) st = LAPY_ERR_BREAKDOWN;
           else if (!isfinite(rr[q]) || !isfinite(rzn[q])) st = LAPY_ERR_NAN;
-          else if (rr[q] <= a.rtol2 * a.bb[s * NP + q]) st = it + 1;
+          else if (RU) {
+            // the FP32 residual fell by delta (or to the tolerance): request an
+            // FP64 update at the next update slot
+            req = (ru_slot && (rr[q] <= a.rtol2 * a.bb[s * NP + q] || rr[q] <= a.delta2 * a.rref[s * NP + q])) ||
+                  rr[q] == S(0);
+            if (!(rzn[q] > S(0)) && !req) st = LAPY_ERR_BREAKDOWN;
+          } else if (rr[q] <= a.rtol2 * a.bb[s * NP + q]) st = it + 1;
           else if (!(rzn[q] > S(0))) st = LAPY_ERR_BREAKDOWN;
         }
         act[q] = st == kActive;
-        beta[q] = act[q] ? (V)(rzn[q] / rz_cur[s * NP + q]) : V(0);
+        beta[q] = (act[q] && rzn[q] > S(0)) ? (V)(rzn[q] / rz_cur[s * NP + q]) : V(0);
         any |= act[q];
         if (first && lane == q) {
           st_nxt[s * NP + q] = st;
           rz_nxt[s * NP + q] = rzn[q];
           if (act[q]) atomicAdd(&a.active[par ^ 1], 1u);
+          if (RU && req) {
+            a.ru_col[(par ^ 1) * (int64_t)a.nseg * NP + s * NP + q] = 1;
+            atomicOr(&a.ru_flag[par ^ 1], 1u);
+          }
         }
       }
       if (any) {
@@ -547,11 +826,10 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
           const int row = a.unit_row[u] + lane;
           if (row < a.unit_row[u + 1]) {
             V z[NP], pv[NP];
-            if (PC == kPrecJacobi) {
-              const V d = a.pc.dinv[row];
-              load_row<V, NP>(a.R, row, z);
-#pragma unroll
-              for (int q = 0; q < NP; ++q) z[q] = d * z[q];
+            if (kDiagPC) {
+              V r[NP];
+              load_row<V, NP>(a.R, row, r);
+              apply_diag_coarse<V, NP, PC>(a, row, r, z);
             } else {
               load_row<V, NP>(a.Z, row, z);
             }
@@ -571,6 +849,20 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
   const int par = it & 1;
   const int32_t* st_fin = a.state + par * (int64_t)a.nseg * NP;
   FOR_MY_PIECES(a, {
+    if (RU) {  // corrections not yet folded in (columns stopped between updates)
+      for (int u = u0; u < u1; ++u) {
+        const int row = a.unit_row[u] + lane;
+        if (row < a.unit_row[u + 1]) {
+          V x[NP];
+          double x64[NP];
+          load_row<V, NP>(a.X, row, x);
+          load_row<double, NP>(a.X64, row, x64);
+#pragma unroll
+          for (int q = 0; q < NP; ++q) x64[q] += (double)x[q];
+          store_row<double, NP>(a.X64, row, x64);
+        }
+      }
+    }
     if (a.seg_piece[s] == p && lane < NP) {
       int32_t st = st_fin[s * NP + lane];
       if (st == kActive) st = LAPY_ERR_NOCONV;
@@ -660,20 +952,24 @@ template int build_sell<float>(int64_t, const int32_t*, const int32_t*, const fl
 template int build_sell<double>(int64_t, const int32_t*, const int32_t*, const double*, const ChunkTable&, void*,
                                 size_t, SellMatrix<double>*, bool*, cudaStream_t);
 
-size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond) {
+size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond, int64_t nagg) {
   const size_t vec = a256((size_t)n * p * elem_size);
   size_t b = vec * (precond == kPrecFactored ? 5 : 3);  // R P Q (+ Z T)
   b += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
   b += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
   b += a256(sizeof(double) * (size_t)ct.nseg * p);
   b += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
-  b += a256(64);  // active[2], iters, barrier, work counters
+  b += a256(64);  // active[2], iters, barrier, work counters, update flags
+  // reliable updates: FP64 partials, reference residuals, request flags
+  b += a256(sizeof(double) * (size_t)ct.npiece * p) + a256(sizeof(double) * (size_t)ct.nseg * p) +
+       a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
+  if (precond == kPrecTwoLevel) b += 3 * a256(sizeof(double) * (size_t)std::max<int64_t>(nagg, 1) * p);
   return b + 256;
 }
 
-template <typename V, int NP, int PC>
+template <typename V, int NP, int PC, bool RU>
 static int launch_pcg(PcgArgs<V>& args, cudaStream_t stream) {
-  auto kern = pcg_kernel<V, NP, PC>;
+  auto kern = pcg_kernel<V, NP, PC, RU>;
   int per_sm = 0;
   LAPY_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPcgThreads, 0));
   if (per_sm <= 0) {
@@ -687,29 +983,32 @@ static int launch_pcg(PcgArgs<V>& args, cudaStream_t stream) {
   return lapy_check_launch("pcg_kernel");
 }
 
-template <typename V, int PC>
+template <typename V, int PC, bool RU = false>
 static int launch_pcg_np(PcgArgs<V>& args, int p, cudaStream_t stream) {
   switch (p) {
-    case 1: return launch_pcg<V, 1, PC>(args, stream);
-    case 2: return launch_pcg<V, 2, PC>(args, stream);
-    case 4: return launch_pcg<V, 4, PC>(args, stream);
-    case 8: return launch_pcg<V, 8, PC>(args, stream);
-    case 16: return launch_pcg<V, 16, PC>(args, stream);
+    case 1: return launch_pcg<V, 1, PC, RU>(args, stream);
+    case 2: return launch_pcg<V, 2, PC, RU>(args, stream);
+    case 4: return launch_pcg<V, 4, PC, RU>(args, stream);
+    case 8: return launch_pcg<V, 8, PC, RU>(args, stream);
+    case 16: return launch_pcg<V, 16, PC, RU>(args, stream);
     default:
       lapy_set_last_message("pcg: block width %d not in {1,2,4,8,16}", p);
       return LAPY_ERR_INVALID;
   }
 }
 
+// Workspace layout and launch shared by the plain and reliable-update solves.
 template <typename V>
-int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals,
-              const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
-              const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
-              cudaStream_t stream, int* iters_out) {
-  if (ws_bytes < pcg_workspace_bytes(n, p, ct, sizeof(V), pc.kind)) return LAPY_ERR_WORKSPACE;
+static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals,
+                   const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
+                   const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
+                   cudaStream_t stream, int* iters_out, const double* K64, const double* B64, double* X64,
+                   double delta, int ru_every, int* updates_out) {
+  if (ws_bytes < pcg_workspace_bytes(n, p, ct, sizeof(V), pc.kind, pc.nagg)) return LAPY_ERR_WORKSPACE;
+  const bool ru = B64 != nullptr;
   char* w = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
   const size_t vec = a256((size_t)n * p * sizeof(V));
-  PcgArgs<V> a;
+  PcgArgs<V> a{};
   a.n = n;
   a.indptr = indptr;
   a.indices = indices;
@@ -741,17 +1040,36 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
   a.rz = (S*)w; w += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
   a.bb = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
   a.state = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
-  unsigned* ctl = (unsigned*)w;  // active[2], iters, count, gen, err, work[2] (u64)
+  unsigned* ctl = (unsigned*)w;  // active[2], iters, count, gen, err, work[2] (u64), ru_flag[2], updates
+  w += a256(64);
   a.active = ctl;
   a.iters = (int*)(ctl + 2);
   a.bar.count = ctl + 3;
   a.bar.gen = ctl + 4;
   a.bar.err = (int*)(ctl + 5);
   a.work = (unsigned long long*)(ctl + 6);
+  a.ru_flag = ctl + 10;
+  a.n_updates = ctl + 12;
+  a.part64 = (double*)w; w += a256(sizeof(double) * (size_t)ct.npiece * p);
+  a.rref = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
+  a.ru_col = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
+  if (pc.kind == kPrecTwoLevel) {
+    const size_t cb = a256(sizeof(double) * (size_t)std::max(pc.nagg, 1) * p);
+    a.rc = (S*)w; w += cb;
+    a.yc = (S*)w; w += cb;
+    a.csl = (S*)w; w += cb;
+  }
   a.state_out = state_dev;
   a.rtol2 = (S)(rtol * rtol);
+  a.rtol2_64 = rtol * rtol;
   a.maxiter = maxiter;
+  a.B64 = B64;
+  a.X64 = X64;
+  a.K64 = K64;
+  a.delta2 = (S)(delta * delta);
+  a.ru_every = std::max(1, ru_every);
   LAPY_CUDA_TRY(cudaMemsetAsync(ctl, 0, 64, stream));
+  if (ru) LAPY_CUDA_TRY(cudaMemsetAsync(a.ru_col, 0, sizeof(int32_t) * 2 * (size_t)ct.nseg * p, stream));
   // segments without rows have no piece: they are reported as solved
   LAPY_CUDA_TRY(cudaMemsetAsync(state_dev, 0, sizeof(int32_t) * (size_t)ct.nseg * p, stream));
   int st;
@@ -762,13 +1080,32 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
     LAPY_CUDA_TRY(cudaEventCreate(&e1));
     LAPY_CUDA_TRY(cudaEventRecord(e0, stream));
   }
-  if (pc.kind == kPrecFactored)
+  if (ru) {
+    if constexpr (sizeof(V) == 4) {
+      if (pc.kind != kPrecJacobi) {
+        lapy_set_last_message("pcg: reliable updates need the Jacobi preconditioner");
+        return LAPY_ERR_INVALID;
+      }
+      st = launch_pcg_np<V, kPrecJacobi, true>(a, p, stream);
+    } else {
+      lapy_set_last_message("pcg: reliable updates run FP32 iterations");
+      return LAPY_ERR_INVALID;
+    }
+  } else if (pc.kind == kPrecFactored) {
     st = launch_pcg_np<V, kPrecFactored>(a, p, stream);
-  else
+  } else if (pc.kind == kPrecTwoLevel) {
+    if constexpr (sizeof(V) == 4) {
+      st = launch_pcg_np<V, kPrecTwoLevel>(a, p, stream);
+    } else {
+      lapy_set_last_message("pcg: the two-level preconditioner runs FP32 iterations");
+      return LAPY_ERR_INVALID;
+    }
+  } else {
     st = launch_pcg_np<V, kPrecJacobi>(a, p, stream);
+  }
   if (st != LAPY_OK) return st;
   if (prof) LAPY_CUDA_TRY(cudaEventRecord(e1, stream));
-  unsigned hctl[10];
+  unsigned hctl[16];
   LAPY_CUDA_TRY(cudaMemcpyAsync(hctl, ctl, sizeof(hctl), cudaMemcpyDeviceToHost, stream));
   LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
   if (prof) {
@@ -786,7 +1123,28 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
     return LAPY_ERR_TIMEOUT;
   }
   if (iters_out) *iters_out = (int)hctl[2];
+  if (updates_out) *updates_out = (int)hctl[12];
   return LAPY_OK;
+}
+
+template <typename V>
+int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals,
+              const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
+              const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
+              cudaStream_t stream, int* iters_out) {
+  return pcg_run<V>(n, indptr, indices, vals, sell, pc, p, ct, B, X, rtol, maxiter, state_dev, ws, ws_bytes,
+                    stream, iters_out, nullptr, nullptr, nullptr, 0.0, 1, nullptr);
+}
+
+int pcg_solve_ru(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64, const float* k32,
+                 const SellMatrix<float>* sell, const float* dinv32, int p, const ChunkTable& ct, const double* B,
+                 double* X, float* X32, double rtol, double delta, int ru_every, int maxiter, int32_t* state_dev,
+                 void* ws, size_t ws_bytes, cudaStream_t stream, int* iters_out, int* updates_out) {
+  PcgPrecondDesc<float> pc;
+  pc.kind = kPrecJacobi;
+  pc.dinv = dinv32;
+  return pcg_run<float>(n, indptr, indices, k32, sell, pc, p, ct, nullptr, X32, rtol, maxiter, state_dev, ws,
+                        ws_bytes, stream, iters_out, k64, B, X, delta, ru_every, updates_out);
 }
 
 template int pcg_solve<float>(int64_t, const int32_t*, const int32_t*, const float*, const SellMatrix<float>*,

@@ -41,7 +41,7 @@ size_t chunk_table_bytes(const ChunkTable& ct);
 // Place the table into `mem` and upload it (synchronous on `stream`).
 int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream);
 
-enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1 };
+enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1, kPrecTwoLevel = 2 };
 
 // Sliced-ELL copy of a CSR matrix: one slice per 32-row unit of a chunk
 // table, entries stored slot-major inside a slice (element k of the slice's
@@ -65,6 +65,9 @@ int build_sell(int64_t n, const int32_t* indptr, const int32_t* indices, const V
 
 // Preconditioner description.  Jacobi: z = dinv .* r.  Factored:
 // z = Gt * (G * r) with G, Gt CSR on the mesh pattern (SPD by construction).
+// Two-level: z = dinv .* r + W (W'KW)^-1 W' r with W the 0/1 aggregation
+// matrix of each segment (disjoint aggregates) and the inverse dense per
+// segment; SPD as the sum of an SPD and a semi-definite term.
 template <typename V>
 struct PcgPrecondDesc {
   int kind = kPrecJacobi;
@@ -75,10 +78,19 @@ struct PcgPrecondDesc {
   const int32_t* gt_ptr = nullptr;
   const int32_t* gt_idx = nullptr;
   const V* gt_val = nullptr;
+  int nagg = 0;                       // aggregates over all segments
+  const int32_t* agg = nullptr;       // n: aggregate of each row (-1: none)
+  const int32_t* agg_ptr = nullptr;   // nagg + 1: member rows of each aggregate
+  const int32_t* agg_row = nullptr;   //   (CSR, rows ascending)
+  const int32_t* agg_sid = nullptr;   // nagg: segment of each aggregate
+  const int32_t* seg_agg = nullptr;   // nseg + 1: aggregate range of each segment
+  const int64_t* kinv_off = nullptr;  // nseg: offset of the segment's nc x nc inverse
+  const float* kinv = nullptr;        // dense (W'KW)^-1 blocks, row-major, FP32
 };
 
-// Scratch needed by one persistent PCG solve of n rows x p columns.
-size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond);
+// Scratch needed by one persistent PCG solve of n rows x p columns (nagg:
+// coarse unknowns of the two-level preconditioner, 0 otherwise).
+size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond, int64_t nagg = 0);
 
 // Per-(segment, column) outcome codes written to `state`:
 //   > 0  converged after that many iterations (1-based)
@@ -91,5 +103,17 @@ int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V*
               const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
               const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
               cudaStream_t stream, int* iters_out);
+
+// Mixed-precision PCG with reliable updates: FP32 Jacobi-PCG iterations
+// (k32 / sell) whose correction is folded into the FP64 solution X, and
+// whose residual is replaced by the FP64 residual B - K64 X, every time the
+// FP32 residual of a (segment, column) has fallen by `delta` (checked every
+// `ru_every` iterations).  The CG direction is kept across updates, so the
+// Krylov recurrence is never restarted.  A column converges when its FP64
+// residual reaches rtol * ||B||.  X32: n x p FP32 scratch.
+int pcg_solve_ru(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64, const float* k32,
+                 const SellMatrix<float>* sell, const float* dinv32, int p, const ChunkTable& ct, const double* B,
+                 double* X, float* X32, double rtol, double delta, int ru_every, int maxiter, int32_t* state_dev,
+                 void* ws, size_t ws_bytes, cudaStream_t stream, int* iters_out, int* updates_out);
 
 }  // namespace lapy

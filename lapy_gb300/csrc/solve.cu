@@ -10,17 +10,23 @@ namespace lapy {
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-size_t ir_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int mixed, int precond) {
+size_t ir_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int mixed, int precond, int64_t nagg) {
   const int nseg = ct.nseg;
   size_t b = 0;
   b += a256(sizeof(double) * n * p);            // R64
   b += a256(sizeof(float) * n * p) * 2;         // R32, D32
   b += a256(sizeof(double) * nseg * p) * 2;     // bn2, rn2
   b += a256(sizeof(int32_t) * nseg * p) * 2;    // state, mask
-  b += mixed ? pcg_workspace_bytes(n, p, ct, sizeof(float), precond)
+  b += mixed ? pcg_workspace_bytes(n, p, ct, sizeof(float), precond, nagg)
              : pcg_workspace_bytes(n, p, ct, sizeof(double), kPrecJacobi);
   return b + 512;
 }
+
+// Reliable updates: fold the FP32 correction in and recompute the FP64
+// residual after each tenfold drop of the FP32 residual, checked every 8
+// iterations.
+constexpr double kReliableDelta = 0.1;
+constexpr int kReliableEvery = 8;
 
 __global__ void mask_cols_kernel(float* __restrict__ R, int p, const int32_t* __restrict__ chunk_row,
                                  const int32_t* __restrict__ chunk_seg, const int32_t* __restrict__ mask) {
@@ -40,7 +46,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
   const int64_t n = K.n;
   const int nsp = ct.nseg * p;
   const int precond = mixed ? K.pc32.kind : kPrecJacobi;
-  if (ws_bytes < ir_workspace_bytes(n, p, ct, mixed, precond)) return LAPY_ERR_WORKSPACE;
+  if (ws_bytes < ir_workspace_bytes(n, p, ct, mixed, precond, mixed ? K.pc32.nagg : 0)) return LAPY_ERR_WORKSPACE;
   char* w = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
   double* R64 = (double*)w; w += a256(sizeof(double) * n * p);
   float* R32 = (float*)w; w += a256(sizeof(float) * n * p);
@@ -78,6 +84,25 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
       else if (hb[i] > 0 && !(hr[i] <= rtol * rtol * hb[i] * 1.0000001)) final_st[i] = LAPY_ERR_NOCONV;
       if (relres2_host) relres2_host[i] = hb[i] > 0 ? hr[i] / hb[i] : 0.0;
     }
+  } else if (K.reliable && K.pc32.kind == kPrecJacobi) {
+    // one launch: FP32 iterations, FP64 solution and residual updates
+    int it = 0, updates = 0;
+    LAPY_TRY(pcg_solve_ru(n, K.indptr, K.indices, K.k64, K.k32, K.sell32.val ? &K.sell32 : nullptr, K.dinv32, p,
+                          ct, B, X, D32, rtol, kReliableDelta, kReliableEvery, maxiter, st, pws, pws_bytes, stream,
+                          &it, &updates));
+    local.rounds = 1;
+    local.pcg_iters = it;
+    LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
+    LAPY_TRY(csr_spmm<double>(n, K.indptr, K.indices, K.k64, p, X, R64, -1.0, 1.0, G, stream));
+    LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
+    LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+    for (int i = 0; i < nsp; ++i) {
+      if (hst[i] < 0) final_st[i] = hst[i];
+      else if (hb[i] > 0 && !(hr[i] <= rtol * rtol * hb[i] * 1.0000001)) final_st[i] = LAPY_ERR_NOCONV;
+      if (relres2_host) relres2_host[i] = hb[i] > 0 ? hr[i] / hb[i] : 0.0;
+    }
   } else {
     LAPY_CUDA_TRY(cudaMemsetAsync(X, 0, sizeof(double) * n * p, stream));
     LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
@@ -96,7 +121,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
       }
       int it = 0;
       PcgPrecondDesc<float> pc = K.pc32;
-      if (pc.kind == kPrecJacobi) pc.dinv = K.dinv32;
+      if (pc.kind != kPrecFactored) pc.dinv = K.dinv32;
       LAPY_TRY(pcg_solve<float>(n, K.indptr, K.indices, K.k32, K.sell32.val ? &K.sell32 : nullptr, pc, p, ct, R32,
                                 D32, round_rtol, maxiter, st, pws, pws_bytes, stream, &it));
       local.rounds++;

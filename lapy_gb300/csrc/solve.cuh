@@ -16,6 +16,9 @@ struct SysMatrix {
   const float* dinv32 = nullptr;
   PcgPrecondDesc<float> pc32;  // kind == kPrecFactored selects the learned/SPAI factor
   SellMatrix<float> sell32;    // SELL copy of k32 (val == nullptr: CSR path)
+  // mixed solves: one reliable-update PCG launch (true, Jacobi only) or
+  // restarted FP32 refinement rounds (false)
+  bool reliable = false;
 };
 
 struct IrStats {
@@ -24,7 +27,7 @@ struct IrStats {
   int status = LAPY_OK;
 };
 
-size_t ir_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int mixed, int precond);
+size_t ir_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int mixed, int precond, int64_t nagg = 0);
 
 // Solve K X = B for p columns (p in {1,2,4,8,16}); X overwritten.  On return
 // relres2[s*p + c] holds ||B - K X||^2 / ||B||^2 (0 for zero columns) and

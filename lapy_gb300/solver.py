@@ -138,8 +138,11 @@ class Solver:
         return A, M.on_pattern(A.indptr, A.indices, A.data.numel()), False
 
     def eigs(self, k: int = 10, sigma: float = -0.01, block: int | None = None, tol: float = 1e-8,
-             inner_rtol: float = 1e-9):
-        """The k eigenpairs of A x = lambda M x nearest ``sigma`` (ascending)."""
+             inner_rtol: float = 1e-9, precond: str = "twolevel"):
+        """The k eigenpairs of A x = lambda M x nearest ``sigma`` (ascending).
+
+        ``precond`` selects the inner PCG's preconditioner: ``"twolevel"``
+        (Jacobi plus an aggregation coarse space) or ``"jacobi"``."""
         A, mvals, m_diag = self._device_pair()
         n = A.n
         if not (0 < k < n):
@@ -148,7 +151,8 @@ class Solver:
         while block > 1 and n < k + 2 * block + 1:
             block //= 2
         evals, evecs, info = eigs_batched(A.indptr, A.indices, A.data.contiguous(), mvals, m_diag,
-                                          np.array([0, n], dtype=np.int32), k, sigma, block, tol, inner_rtol)
+                                          np.array([0, n], dtype=np.int32), k, sigma, block, tol, inner_rtol,
+                                          precond=precond)
         st = int(info["status"][0])
         if st != 0:
             _lib.check(st, "Solver.eigs")
@@ -248,18 +252,21 @@ class Solver:
 
 def eigs_batched(indptr, indices, a_vals, m_vals, m_is_diag: bool, seg_row, k: int, sigma: float = -0.01,
                  block: int = DEFAULT_BLOCK, tol: float = 1e-8, inner_rtol: float = 1e-9, inner_maxiter: int = 20000,
-                 max_vectors: int | None = None, seed: int = 1234):
+                 max_vectors: int | None = None, seed: int = 1234, precond: str = "twolevel"):
     """Shift-invert eigenpairs of every segment of a block-diagonal batch.
 
     Returns (evals: nseg x k tensor, evecs: n x k tensor, info dict)."""
     L = _lib.lib()
+    pc = {"jacobi": _lib.PRECOND_JACOBI, "twolevel": _lib.PRECOND_TWO_LEVEL}.get(precond)
+    if pc is None:
+        raise ValueError(f"precond must be 'jacobi' or 'twolevel', not {precond!r}")
     seg_row = np.ascontiguousarray(seg_row, dtype=np.int32)
     nseg = len(seg_row) - 1
     n = int(seg_row[-1])
     nnz = int(a_vals.numel())
     if max_vectors is None:
         max_vectors = 6 * k + 8 * block
-    ws_bytes = L.lapy_eigs_workspace_bytes(n, nnz, nseg, seg_row.ctypes.data, k, block, max_vectors)
+    ws_bytes = L.lapy_eigs_workspace_bytes(n, nnz, nseg, seg_row.ctypes.data, k, block, max_vectors, pc)
     ws = workspace(ws_bytes)
     evals = torch.empty(nseg, k, dtype=torch.float64, device="cuda")
     evecs = torch.empty(n, k, dtype=torch.float64, device="cuda")
@@ -268,9 +275,9 @@ def eigs_batched(indptr, indices, a_vals, m_vals, m_is_diag: bool, seg_row, k: i
     iters = C.c_int64(0)
     _lib.check(L.lapy_eigs_shift_invert(n, dptr(indptr), dptr(indices), dptr(a_vals), dptr(m_vals), int(m_is_diag),
                                         nnz, nseg, seg_row.ctypes.data, sigma, k, block, max_vectors, tol, inner_rtol,
-                                        inner_maxiter, seed, dptr(evals), dptr(evecs), status.ctypes.data,
+                                        inner_maxiter, pc, seed, dptr(evals), dptr(evecs), status.ctypes.data,
                                         nbasis.ctypes.data, C.byref(iters), dptr(ws), ws.numel(), stream()),
                "eigs_shift_invert")
-    info = {"status": status, "nbasis": nbasis, "inner_iters": int(iters.value), "block": block,
+    info = {"status": status, "nbasis": nbasis, "inner_iters": int(iters.value), "block": block, "precond": precond,
             "workspace_bytes": int(ws_bytes)}
     return evals, evecs, info
