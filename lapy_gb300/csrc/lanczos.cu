@@ -116,6 +116,98 @@ __global__ void __launch_bounds__(256) gemm_nn_kernel(BMat X, int na, const doub
   }
 }
 
+// Block-row forms of the two basis products for a basis stored as blocks of P
+// columns (block j: n x P row-major at X + j * bst), one thread per row.
+//
+// TN: partial[c][j*P + a][b] = sum over chunk c's rows of X_j(row, a) Y(row, b)
+// for JB consecutive blocks per CTA (grid.y), accumulated in registers and
+// reduced over the CTA in a fixed order.
+template <int P, int JB>
+__global__ void __launch_bounds__(256) gemm_tn_blk_kernel(const double* __restrict__ X, int64_t bst, int nblk,
+                                                          const double* __restrict__ Y,
+                                                          const int32_t* __restrict__ chunk_row,
+                                                          const int32_t* __restrict__ chunk_seg,
+                                                          const int32_t* __restrict__ active,
+                                                          double* __restrict__ partial) {
+  constexpr int NV = JB * P * P;
+  __shared__ double red[8][NV];
+  const int c = blockIdx.x, j0 = blockIdx.y * JB;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) acc[v] = 0.0;
+  if (!active || active[chunk_seg[c]]) {
+    const int64_t r1 = chunk_row[c + 1];
+    for (int64_t r = chunk_row[c] + threadIdx.x; r < r1; r += blockDim.x) {
+      double y[P];
+#pragma unroll
+      for (int b = 0; b < P; ++b) y[b] = __ldg(Y + r * P + b);
+#pragma unroll
+      for (int jj = 0; jj < JB; ++jj) {
+        if (j0 + jj < nblk) {
+          const double* xr = X + (int64_t)(j0 + jj) * bst + r * P;
+#pragma unroll
+          for (int a = 0; a < P; ++a) {
+            const double x = __ldg(xr + a);
+#pragma unroll
+            for (int b = 0; b < P; ++b) acc[(jj * P + a) * P + b] = fma(x, y[b], acc[(jj * P + a) * P + b]);
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const double t = warp_sum(acc[v]);
+    if (lane == 0) red[warp][v] = t;
+  }
+  __syncthreads();
+  const int na = nblk * P;
+  for (int v = threadIdx.x; v < NV; v += blockDim.x) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][v];
+    const int jj = v / (P * P), a = (v / P) % P, b = v % P;
+    if (j0 + jj < nblk) partial[((int64_t)c * na + (j0 + jj) * P + a) * P + b] = t;
+  }
+}
+
+// NN: Y(row, b) = beta Y(row, b) + alpha sum_j sum_a X_j(row, a) H_s[j*P + a][b]
+// with the segment's H (nblk*P x P) staged in shared memory.
+template <int P>
+__global__ void __launch_bounds__(256) gemm_nn_blk_kernel(const double* __restrict__ X, int64_t bst, int nblk,
+                                                          const double* __restrict__ H, int64_t h_seg_stride,
+                                                          int ldh, double* __restrict__ Y, double alpha, double beta,
+                                                          const int32_t* __restrict__ chunk_row,
+                                                          const int32_t* __restrict__ chunk_seg,
+                                                          const int32_t* __restrict__ active) {
+  extern __shared__ double hsm[];
+  const int c = blockIdx.x;
+  const int s = chunk_seg[c];
+  if (active && !active[s]) return;
+  const double* Hs = H + (int64_t)s * h_seg_stride;
+  for (int i = threadIdx.x; i < nblk * P * P; i += blockDim.x) hsm[i] = Hs[(int64_t)(i / P) * ldh + (i % P)];
+  __syncthreads();
+  const int64_t r1 = chunk_row[c + 1];
+  for (int64_t r = chunk_row[c] + threadIdx.x; r < r1; r += blockDim.x) {
+    double acc[P];
+#pragma unroll
+    for (int b = 0; b < P; ++b) acc[b] = 0.0;
+    for (int j = 0; j < nblk; ++j) {
+      const double* xr = X + (int64_t)j * bst + r * P;
+      const double* hj = hsm + j * P * P;
+#pragma unroll
+      for (int a = 0; a < P; ++a) {
+        const double x = __ldg(xr + a);
+#pragma unroll
+        for (int b = 0; b < P; ++b) acc[b] = fma(x, hj[a * P + b], acc[b]);
+      }
+    }
+    double* yr = Y + r * P;
+#pragma unroll
+    for (int b = 0; b < P; ++b) yr[b] = (beta == 0.0) ? alpha * acc[b] : beta * yr[b] + alpha * acc[b];
+  }
+}
+
 // Cholesky of the p x p Gram matrix of every segment: G = R' R (R upper).
 // Inactive segments get R = I.  fail[s] = 1 when G is not numerically SPD.
 __global__ void chol_small_kernel(int nseg, int p, const double* __restrict__ G, double* __restrict__ R,
@@ -365,6 +457,7 @@ struct EigPtrs {
   double* basis; double* Y; double* W; double* MW;
   void* ir_ws; size_t ir_bytes;
   void* sell_mem; size_t sell_bytes;
+  void* sell64_mem; void* sellm_mem; size_t sell64_bytes;
   void* tl_mem; size_t tl_bytes;
   double* partial;
   double* H; double* Hsum; double* G; double* R1; double* R2; double* Bm;
@@ -415,6 +508,9 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.tl_mem = take(e.tl_bytes);
   e.sell_bytes = sell_bytes_bound(nnz, P.ct, sizeof(float));
   e.sell_mem = take(e.sell_bytes);
+  e.sell64_bytes = sell_bytes_bound(nnz, P.ct, sizeof(double));
+  e.sell64_mem = take(e.sell64_bytes);
+  e.sellm_mem = take(e.sell64_bytes);
   const size_t part_elems = (size_t)P.gt.nchunk * std::max((size_t)lda * p, (size_t)keff * keff);
   e.partial = (double*)take(8 * part_elems);
   e.H = (double*)take(8 * (size_t)ns * lda * p);
@@ -458,24 +554,60 @@ struct EigOps {
   int m_is_diag;
   int G;
   cudaStream_t st;
+  SellMatrix<double> sellM;  // SELL copy of a consistent M (val == nullptr: CSR)
 
   int apply_M(const double* X, double* Y, int ncol) const {
     if (m_is_diag) {
       return lapy_diag_mm_f64(P.n, m_vals, ncol, X, Y, 1.0, 0.0, st);
     }
+    if (sellM.val && sell_spmm<double>(sellM, P.ct.nunit, P.ct.unit_row, ncol, X, Y, 1.0, 0.0, st) == LAPY_OK)
+      return LAPY_OK;
     return csr_spmm<double>(P.n, indptr, indices, m_vals, ncol, X, Y, 1.0, 0.0, G, st);
   }
   // out_s (na x nb, ldo) = X' Y per segment
+  template <int PB, int JB>
+  int gemm_tn_blk(BMat X, int na, BMat Y, const int32_t* act) const {
+    const int nblk = na / PB;
+    dim3 grid(P.gt.nchunk, lapy_ceil_div(nblk, JB));
+    gemm_tn_blk_kernel<PB, JB><<<grid, 256, 0, st>>>(X.base, X.bst, nblk, Y.base, P.gt.chunk_row, P.gt.chunk_seg,
+                                                     act, e.partial);
+    return lapy_check_launch("gemm_tn_blk_kernel");
+  }
   int gemm_tn(BMat X, int na, BMat Y, int nb, double* out, int64_t out_stride, int ldo, const int32_t* act) const {
-    dim3 grid(P.gt.nchunk, lapy_ceil_div(na, kTile), lapy_ceil_div(nb, kTile));
-    gemm_tn_partial_kernel<<<grid, 256, 0, st>>>(X, na, Y, nb, P.gt.chunk_row, P.gt.chunk_seg, act, e.partial);
-    LAPY_TRY(lapy_check_launch("gemm_tn_partial_kernel"));
+    const bool blk = X.bs == nb && Y.bs == nb && Y.bst == 0 && na % nb == 0;
+    if (blk && nb == 1) {
+      LAPY_TRY((gemm_tn_blk<1, 16>(X, na, Y, act)));
+    } else if (blk && nb == 2) {
+      LAPY_TRY((gemm_tn_blk<2, 8>(X, na, Y, act)));
+    } else if (blk && nb == 4) {
+      LAPY_TRY((gemm_tn_blk<4, 2>(X, na, Y, act)));
+    } else if (blk && nb == 8) {
+      LAPY_TRY((gemm_tn_blk<8, 1>(X, na, Y, act)));
+    } else {
+      dim3 grid(P.gt.nchunk, lapy_ceil_div(na, kTile), lapy_ceil_div(nb, kTile));
+      gemm_tn_partial_kernel<<<grid, 256, 0, st>>>(X, na, Y, nb, P.gt.chunk_row, P.gt.chunk_seg, act, e.partial);
+      LAPY_TRY(lapy_check_launch("gemm_tn_partial_kernel"));
+    }
     dim3 g2(P.nseg, std::max(1u, std::min(64u, lapy_ceil_div((int64_t)na * nb, 256))));
     gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, na, nb, P.gt.seg_chunk, out, out_stride, ldo);
     return lapy_check_launch("gemm_tn_reduce_kernel");
   }
+  template <int PB>
+  int gemm_nn_blk(BMat X, int na, const double* H, int64_t hs, int ldh, double* Y, double alpha, double beta,
+                  const int32_t* act) const {
+    const int nblk = na / PB;
+    const size_t smem = sizeof(double) * (size_t)nblk * PB * PB;
+    gemm_nn_blk_kernel<PB><<<P.gt.nchunk, 256, smem, st>>>(X.base, X.bst, nblk, H, hs, ldh, Y, alpha, beta,
+                                                            P.gt.chunk_row, P.gt.chunk_seg, act);
+    return lapy_check_launch("gemm_nn_blk_kernel");
+  }
   int gemm_nn(BMat X, int na, const double* H, int64_t hs, int ldh, double* Y, int ldy, int nb, double alpha,
               double beta, const int32_t* act) const {
+    const bool blk = X.bs == nb && ldy == nb && na % nb == 0 && sizeof(double) * (size_t)na * nb <= 48 * 1024;
+    if (blk && nb == 1) return gemm_nn_blk<1>(X, na, H, hs, ldh, Y, alpha, beta, act);
+    if (blk && nb == 2) return gemm_nn_blk<2>(X, na, H, hs, ldh, Y, alpha, beta, act);
+    if (blk && nb == 4) return gemm_nn_blk<4>(X, na, H, hs, ldh, Y, alpha, beta, act);
+    if (blk && nb == 8) return gemm_nn_blk<8>(X, na, H, hs, ldh, Y, alpha, beta, act);
     gemm_nn_kernel<<<P.gt.nchunk, 256, 0, st>>>(X, na, H, hs, ldh, Y, ldy, nb, alpha, beta, P.gt.chunk_row,
                                                P.gt.chunk_seg, act);
     return lapy_check_launch("gemm_nn_kernel");
@@ -513,7 +645,7 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   const int64_t n = P.n;
   const int p = P.p, ns = P.nseg, keff = P.keff, lda = P.lda, k = P.k;
   const int G = spmm_pick_group(n, P.nnz);
-  EigOps ops{P, e, indptr, indices, a_vals, m_vals, m_is_diag, G, st};
+  EigOps ops{P, e, indptr, indices, a_vals, m_vals, m_is_diag, G, st, SellMatrix<double>()};
   ChunkTable ct = P.ct, gt = P.gt;
   LAPY_TRY(upload_chunk_table(&ct, e.ct_mem, st));
   LAPY_TRY(upload_chunk_table(&gt, e.gt_mem, st));
@@ -537,6 +669,16 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     bool fits = false;
     LAPY_TRY(build_sell<float>(n, indptr, indices, e.k32, P.ct, e.sell_mem, e.sell_bytes, &K.sell32, &fits, st));
     if (!fits) K.sell32 = SellMatrix<float>();
+  }
+  {
+    bool fits = false;
+    LAPY_TRY(build_sell<double>(n, indptr, indices, e.k64, P.ct, e.sell64_mem, e.sell64_bytes, &K.sell64, &fits, st));
+    if (!fits) K.sell64 = SellMatrix<double>();
+    if (!m_is_diag) {
+      LAPY_TRY(build_sell<double>(n, indptr, indices, m_vals, P.ct, e.sellm_mem, e.sell64_bytes, &ops.sellM, &fits,
+                                  st));
+      if (!fits) ops.sellM = SellMatrix<double>();
+    }
   }
   if (P.precond == kPrecTwoLevel)
     LAPY_TRY(build_two_level(n, indptr, indices, e.k64, P.ct.h_seg_row.data(), ns, e.tl_mem, e.tl_bytes, &K.pc32, st));

@@ -39,6 +39,14 @@ __global__ void mask_cols_kernel(float* __restrict__ R, int p, const int32_t* __
   }
 }
 
+// R -= K X in FP64 (R holds B on entry): the SELL copy when present.
+static int residual64(const SysMatrix& K, const ChunkTable& ct, int p, const double* X, double* R, int G,
+                      cudaStream_t stream) {
+  if (K.sell64.val && sell_spmm<double>(K.sell64, ct.nunit, ct.unit_row, p, X, R, -1.0, 1.0, stream) == LAPY_OK)
+    return LAPY_OK;
+  return csr_spmm<double>(K.n, K.indptr, K.indices, K.k64, p, X, R, -1.0, 1.0, G, stream);
+}
+
 int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, double* X,
              double rtol, int maxiter, int mixed, double inner_rtol, int max_rounds, void* ws,
              size_t ws_bytes, cudaStream_t stream, IrStats* stats, double* relres2_host,
@@ -75,7 +83,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
     local.pcg_iters = it;
     LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));
     LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
-    LAPY_TRY(csr_spmm<double>(n, K.indptr, K.indices, K.k64, p, X, R64, -1.0, 1.0, G, stream));
+    LAPY_TRY(residual64(K, ct, p, X, R64, G, stream));
     LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
     LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
     LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -94,7 +102,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
     local.pcg_iters = it;
     LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));
     LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
-    LAPY_TRY(csr_spmm<double>(n, K.indptr, K.indices, K.k64, p, X, R64, -1.0, 1.0, G, stream));
+    LAPY_TRY(residual64(K, ct, p, X, R64, G, stream));
     LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
     LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
     LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -128,7 +136,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
       local.pcg_iters += it;
       LAPY_TRY(add_f32_to_f64(n * p, D32, X, stream));
       LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
-      LAPY_TRY(csr_spmm<double>(n, K.indptr, K.indices, K.k64, p, X, R64, -1.0, 1.0, G, stream));
+      LAPY_TRY(residual64(K, ct, p, X, R64, G, stream));
       LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
       LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
       LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));

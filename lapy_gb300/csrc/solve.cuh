@@ -16,6 +16,7 @@ struct SysMatrix {
   const float* dinv32 = nullptr;
   PcgPrecondDesc<float> pc32;  // kind == kPrecFactored selects the learned/SPAI factor
   SellMatrix<float> sell32;    // SELL copy of k32 (val == nullptr: CSR path)
+  SellMatrix<double> sell64;   // SELL copy of k64 for the FP64 residuals (optional)
   // mixed solves: one reliable-update PCG launch (true, Jacobi only) or
   // restarted FP32 refinement rounds (false)
   bool reliable = false;

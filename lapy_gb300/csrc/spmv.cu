@@ -78,6 +78,64 @@ __global__ void diag_mm_kernel(int64_t n, const double* __restrict__ d, int ncol
   y[i] = (beta == 0.0) ? v : v + beta * y[i];
 }
 
+
+// ---- SELL (sliced ELL, 32-row slices) product, lane = row -----------------
+template <typename V, int NP>
+__global__ void __launch_bounds__(256) sell_spmm_kernel(int nunit, const int32_t* __restrict__ unit_row,
+                                                        const int32_t* __restrict__ slice_ptr,
+                                                        const int32_t* __restrict__ col, const V* __restrict__ val,
+                                                        const V* __restrict__ x, V* __restrict__ y, V alpha, V beta) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunit; u += nw) {
+    const int32_t base = slice_ptr[u];
+    const int w = (slice_ptr[u + 1] - base) >> 5;
+    V acc[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) acc[q] = V(0);
+#pragma unroll 4
+    for (int k = 0; k < w; ++k) {
+      const V a = __ldg(val + base + 32 * k + lane);
+      const V* xr = x + (int64_t)__ldg(col + base + 32 * k + lane) * NP;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] += a * __ldg(xr + q);
+    }
+    const int64_t row = unit_row[u] + lane;
+    if (row < unit_row[u + 1]) {
+      V* yr = y + row * NP;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) yr[q] = (beta == V(0)) ? alpha * acc[q] : alpha * acc[q] + beta * yr[q];
+    }
+  }
+}
+
+template <typename V>
+int sell_spmm(const SellMatrix<V>& M, int nunit, const int32_t* unit_row, int ncol, const V* x, V* y, V alpha,
+              V beta, cudaStream_t stream) {
+  if (!M.val || nunit <= 0) return LAPY_ERR_INVALID;
+  const unsigned grid = std::min<unsigned>(lapy_ceil_div((int64_t)nunit * 32, 256), 8u * lapy_num_sms());
+#define LAPY_SELL_CASE(NPV)                                                                                  \
+  case NPV:                                                                                                \
+    sell_spmm_kernel<V, NPV><<<grid, 256, 0, stream>>>(nunit, unit_row, M.slice_ptr, M.col, M.val, x, y, alpha, \
+                                                       beta);                                              \
+    return lapy_check_launch("sell_spmm_kernel");
+  switch (ncol) {
+    LAPY_SELL_CASE(1)
+    LAPY_SELL_CASE(2)
+    LAPY_SELL_CASE(4)
+    LAPY_SELL_CASE(8)
+    LAPY_SELL_CASE(16)
+    default:
+      return LAPY_ERR_INVALID;
+  }
+#undef LAPY_SELL_CASE
+}
+
+template int sell_spmm<double>(const SellMatrix<double>&, int, const int32_t*, int, const double*, double*, double,
+                               double, cudaStream_t);
+template int sell_spmm<float>(const SellMatrix<float>&, int, const int32_t*, int, const float*, float*, float, float,
+                              cudaStream_t);
+
 }  // namespace lapy
 
 using namespace lapy;

@@ -1,6 +1,7 @@
 // CSR sparse x dense (row-major n x ncol) products.
 #pragma once
 #include "common.cuh"
+#include "pcg.cuh"
 
 namespace lapy {
 
@@ -37,5 +38,12 @@ __device__ __forceinline__ void row_dot_group(const int32_t* __restrict__ indptr
     for (int o = G / 2; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o, G);
   }
 }
+
+// Y = alpha * Mat * X + beta * Y from a SELL copy (one warp per 32-row unit,
+// lane = row; ncol in {1, 2, 4, 8, 16}).  Returns LAPY_ERR_INVALID for other
+// widths (callers then use csr_spmm).
+template <typename V>
+int sell_spmm(const SellMatrix<V>& M, int nunit, const int32_t* unit_row, int ncol, const V* x, V* y, V alpha,
+              V beta, cudaStream_t stream);
 
 }  // namespace lapy
