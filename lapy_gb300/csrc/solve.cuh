@@ -18,7 +18,9 @@ struct SysMatrix {
   SellMatrix<float> sell32;    // SELL copy of k32 (val == nullptr: CSR path)
   SellMatrix<double> sell64;   // SELL copy of k64 for the FP64 residuals (optional)
   // mixed solves: one reliable-update PCG launch (true, Jacobi only) or
-  // restarted FP32 refinement rounds (false)
+  // restarted FP32 refinement rounds (false).  Keeping the CG direction
+  // across residual replacements stagnates on some right-hand sides (FP32
+  // iterates), so the restarted rounds are the default.
   bool reliable = false;
 };
 
