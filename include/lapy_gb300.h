@@ -232,6 +232,61 @@ int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const int32_t* indi
                            int32_t* status_out, int32_t* nbasis_out, int64_t* inner_iters_out,
                            void* ws, size_t ws_bytes, void* stream);
 
+/* ---- learned sparse approximate inverse (per-edge MLP) -------------------
+ * No counterpart in the reference (it factorises with splu).  For an SPD
+ * system K on a symmetric mesh pattern, G is lower triangular on the lower
+ * pattern; a per-edge network (6 -> 64 -> 64 -> 1, tanh, BF16 weights, FP32
+ * arithmetic, parameter layout W1[64][6] b1[64] W2[64][64] b2[64] W3[64] b3)
+ * emits w_ij for every lower entry, and
+ *   q_i = (e_i - w_i)' K (e_i - w_i), G_ii = q_i^-1/2, G_ij = -w_ij G_ii,
+ * so z = G' G r is SPD for every w (w = 0 is Jacobi).  Training minimises
+ * sum_i log q_i (the Kaporin functional of G K G').
+ *
+ * Pattern: lower entries (col <= row, diagonal last; lpos = CSR position of
+ * each) and upper entries (col >= row) with umap = lower index of the
+ * transposed entry; each has (nnz + n) / 2 entries. */
+int lapy_spai_param_count(void);
+size_t lapy_spai_pattern_workspace_bytes(int64_t n);
+int lapy_spai_pattern(int64_t n, const int32_t* indptr, const int32_t* indices, int64_t nnz,
+                      int32_t* lptr, int32_t* lcol, int32_t* lpos, int32_t* uptr, int32_t* ucol,
+                      int32_t* umap, void* work, size_t ws_bytes, void* stream);
+/* Edge features (6 floats per lower entry): -A_ij, |v_i - v_j| / h, m_i / h^2,
+ * m_j / h^2, log(t / h^2), sigma, with m the lumped mass (row sums of M, or M
+ * itself when m_is_diag) and per-segment t, sigma, h (device arrays, nseg).
+ * mass_work: n doubles of scratch. */
+int lapy_spai_features(int64_t n, int nseg, const int32_t* seg_row, const void* v, int coords_f32,
+                       const int32_t* indptr, const double* a_vals, const double* m_vals,
+                       int m_is_diag, const int32_t* lptr, const int32_t* lcol, const int32_t* lpos,
+                       const double* t_seg, const double* sigma_seg, const double* h_seg,
+                       double* mass_work, float* feat, void* stream);
+/* w_out[e] = network(feat[e]) for ne entries; weights: lapy_spai_param_count() bf16. */
+int lapy_spai_forward(int64_t ne, const float* feat, const void* weights_bf16, float* w_out, void* stream);
+/* G on the lower pattern (FP32), log q_i per row and dL/dw per entry (either
+ * output may be NULL); k_vals: K (FP64) on the CSR pattern. */
+int lapy_spai_factor(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
+                     const int32_t* lptr, const int32_t* lcol, const int32_t* lpos, const float* w,
+                     float* g_lower, double* logq, float* dldw, void* stream);
+/* G' values on the upper pattern: g_upper[u] = g_lower[umap[u]] (m upper entries). */
+int lapy_spai_transpose_values(int64_t m, const int32_t* umap, const float* g_lower, float* g_upper,
+                               void* stream);
+/* grad = scale * sum_e dldw[e] * d network(feat[e]) / d parameters (FP32,
+ * straight through the BF16 rounding), reduced in a fixed order. */
+size_t lapy_spai_backward_workspace_bytes(int64_t ne);
+int lapy_spai_backward(int64_t ne, const float* feat, const void* weights_bf16, const float* dldw,
+                       float scale, float* grad, void* work, size_t ws_bytes, void* stream);
+/* One Adam step on the FP32 master parameters; refreshes the BF16 copy. */
+int lapy_spai_adam(int nparam, float* theta, const float* grad, float* m, float* v, void* weights_bf16,
+                   float lr, float beta1, float beta2, float eps, int step, void* stream);
+int lapy_spai_weights_to_bf16(int nparam, const float* theta, void* weights_bf16, void* stream);
+/* lapy_pcg_solve (mixed precision) with z = G' (G r) instead of Jacobi. */
+size_t lapy_spai_pcg_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, int ncol);
+int lapy_spai_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
+                        int64_t nnz, int nseg, const int32_t* seg_row, int ncol, const double* b,
+                        double* x, double rtol, int maxiter, double inner_rtol, const int32_t* lptr,
+                        const int32_t* lcol, const float* g_lower, const int32_t* uptr,
+                        const int32_t* ucol, const float* g_upper, int32_t* status_out,
+                        double* relres_out, int64_t* iters_out, void* ws, size_t ws_bytes, void* stream);
+
 /* ---- heat-method geodesics (lapy/diffgeo.py) ----------------------------
  * Gradient per element of nf vertex functions f (row-major n x nf) into
  * out (m x nf x 3): tria_compute_gradient (diffgeo.py:222-300) and

@@ -81,6 +81,21 @@ _SIGNATURES = {
                               _vp, _vp, C.POINTER(_i64), _vp, _sz, _vp]),
     "lapy_pcg_solve_static": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _dbl, _int, _int,
                                      _dbl, _vp, _vp, C.POINTER(_i64), _vp]),
+    "lapy_spai_param_count": (_int, []),
+    "lapy_spai_pattern_workspace_bytes": (_sz, [_i64]),
+    "lapy_spai_pattern": (_int, [_i64, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "lapy_spai_features": (_int, [_i64, _int, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp,
+                                  _vp, _vp, _vp]),
+    "lapy_spai_forward": (_int, [_i64, _vp, _vp, _vp, _vp]),
+    "lapy_spai_factor": (_int, [_i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "lapy_spai_transpose_values": (_int, [_i64, _vp, _vp, _vp, _vp]),
+    "lapy_spai_backward_workspace_bytes": (_sz, [_i64]),
+    "lapy_spai_backward": (_int, [_i64, _vp, _vp, _vp, C.c_float, _vp, _vp, _sz, _vp]),
+    "lapy_spai_adam": (_int, [_int, _vp, _vp, _vp, _vp, _vp, C.c_float, C.c_float, C.c_float, C.c_float, _int, _vp]),
+    "lapy_spai_weights_to_bf16": (_int, [_int, _vp, _vp, _vp]),
+    "lapy_spai_pcg_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int]),
+    "lapy_spai_pcg_solve": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _dbl, _int, _dbl, _vp, _vp,
+                                   _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(_i64), _vp, _sz, _vp]),
     "lapy_eigs_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int, _int, _int, _int]),
     "lapy_eigs_shift_invert": (_int, [_i64, _vp, _vp, _vp, _vp, _int, _i64, _int, _vp, _dbl, _int, _int,
                                       _int, _dbl, _dbl, _int, _int, C.c_uint64, _vp, _vp, _vp, _vp,

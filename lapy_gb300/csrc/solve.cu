@@ -239,7 +239,7 @@ static int next_pow2_le16(int c) {
   return p;
 }
 
-static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed, char* base,
+static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed, int precond, char* base,
                            int32_t** diag_pos, double** dinv64, float** dinv32, float** k32,
                            double** Bp, double** Xp, void** chunk_mem, void** ir_ws, size_t* ir_bytes,
                            void** sell_mem, size_t* sell_bytes, int* nchunk_out, ChunkTable* ct_plan,
@@ -262,7 +262,7 @@ static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed
   char* p4 = take(sizeof(double) * n * p);
   char* p5 = take(sizeof(double) * n * p);
   char* p6 = take(chunk_table_bytes(ct));
-  const size_t irb = ir_workspace_bytes(n, p, ct, mixed, kPrecJacobi);
+  const size_t irb = ir_workspace_bytes(n, p, ct, mixed, precond);
   char* p7 = take(irb);
   const size_t sellb = mixed ? sell_bytes_bound(nnz, ct, sizeof(float)) : 0;
   char* p8 = take(sellb);
@@ -287,16 +287,18 @@ static size_t solve_layout(int64_t n, int64_t nnz, int nseg, int ncol, int mixed
 extern "C" size_t lapy_pcg_solve_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row,
                                                  int ncol, int mixed) {
   if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0) return 0;
-  return solve_layout(n, nnz, nseg, ncol, mixed, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+  return solve_layout(n, nnz, nseg, ncol, mixed, kPrecJacobi, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
                       nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row);
 }
 
-extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices,
-                              const double* k_vals, int64_t nnz, int nseg, const int32_t* seg_row,
-                              int ncol, const double* b, double* x, double rtol, int maxiter, int mixed,
-                              double inner_rtol, int32_t* status_out, double* relres_out,
-                              int64_t* iters_out, void* ws, size_t ws_bytes, void* stream_) {
-  cudaStream_t stream = (cudaStream_t)stream_;
+// Shared body of the PCG entry points; `factored` (may be null) selects the
+// factored preconditioner z = G' (G r) with FP32 factors on CSR patterns.
+static int pcg_solve_impl(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
+                          int64_t nnz, int nseg, const int32_t* seg_row, int ncol, const double* b, double* x,
+                          double rtol, int maxiter, int mixed, double inner_rtol, int32_t* status_out,
+                          double* relres_out, int64_t* iters_out, void* ws, size_t ws_bytes, cudaStream_t stream,
+                          const PcgPrecondDesc<float>* factored) {
+  const int precond = factored ? kPrecFactored : kPrecJacobi;
   if (n <= 0 || !indptr || !indices || !k_vals || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0 ||
       !b || !x || !(rtol > 0) || maxiter <= 0 || !ws) {
     lapy_set_last_message("pcg_solve: invalid arguments");
@@ -306,7 +308,10 @@ extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* i
     lapy_set_last_message("pcg_solve: segment rows must span [0, n)");
     return LAPY_ERR_INVALID;
   }
-  if (ws_bytes < lapy_pcg_solve_workspace_bytes(n, nnz, nseg, seg_row, ncol, mixed)) return LAPY_ERR_WORKSPACE;
+  if (ws_bytes < solve_layout(n, nnz, nseg, ncol, mixed, precond, nullptr, nullptr, nullptr, nullptr, nullptr,
+                              nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                              seg_row))
+    return LAPY_ERR_WORKSPACE;
   int32_t* diag_pos;
   double *dinv64, *Bp, *Xp;
   float *dinv32, *k32;
@@ -315,7 +320,7 @@ extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* i
   int nchunk;
   ChunkTable ct;
   char* base = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
-  solve_layout(n, nnz, nseg, ncol, mixed, base, &diag_pos, &dinv64, &dinv32, &k32, &Bp, &Xp, &chunk_mem,
+  solve_layout(n, nnz, nseg, ncol, mixed, precond, base, &diag_pos, &dinv64, &dinv32, &k32, &Bp, &Xp, &chunk_mem,
                &ir_ws, &ir_bytes, &sell_mem, &sell_bytes, &nchunk, &ct, seg_row);
   LAPY_TRY(upload_chunk_table(&ct, chunk_mem, stream));
   LAPY_TRY(lapy_csr_diag_index(n, indptr, indices, diag_pos, stream));
@@ -330,6 +335,7 @@ extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* i
   K.k32 = k32;
   K.dinv64 = dinv64;
   K.dinv32 = dinv32;
+  if (factored) K.pc32 = *factored;
   if (mixed) {
     bool fits = false;
     LAPY_TRY(build_sell<float>(n, indptr, indices, k32, ct, sell_mem, sell_bytes, &K.sell32, &fits, stream));
@@ -356,6 +362,45 @@ extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* i
   LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
   if (iters_out) *iters_out = total_iters;
   return LAPY_OK;
+}
+
+extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices,
+                              const double* k_vals, int64_t nnz, int nseg, const int32_t* seg_row,
+                              int ncol, const double* b, double* x, double rtol, int maxiter, int mixed,
+                              double inner_rtol, int32_t* status_out, double* relres_out,
+                              int64_t* iters_out, void* ws, size_t ws_bytes, void* stream) {
+  return pcg_solve_impl(n, indptr, indices, k_vals, nnz, nseg, seg_row, ncol, b, x, rtol, maxiter, mixed,
+                        inner_rtol, status_out, relres_out, iters_out, ws, ws_bytes, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" size_t lapy_spai_pcg_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row,
+                                                int ncol) {
+  if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0) return 0;
+  return solve_layout(n, nnz, nseg, ncol, 1, kPrecFactored, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row);
+}
+
+extern "C" int lapy_spai_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
+                                   int64_t nnz, int nseg, const int32_t* seg_row, int ncol, const double* b,
+                                   double* x, double rtol, int maxiter, double inner_rtol, const int32_t* lptr,
+                                   const int32_t* lcol, const float* g_lower, const int32_t* uptr,
+                                   const int32_t* ucol, const float* g_upper, int32_t* status_out,
+                                   double* relres_out, int64_t* iters_out, void* ws, size_t ws_bytes,
+                                   void* stream) {
+  if (!lptr || !lcol || !g_lower || !uptr || !ucol || !g_upper) {
+    lapy_set_last_message("spai_pcg_solve: missing factor arrays");
+    return LAPY_ERR_INVALID;
+  }
+  PcgPrecondDesc<float> pc;
+  pc.kind = kPrecFactored;
+  pc.g_ptr = lptr;
+  pc.g_idx = lcol;
+  pc.g_val = g_lower;
+  pc.gt_ptr = uptr;
+  pc.gt_idx = ucol;
+  pc.gt_val = g_upper;
+  return pcg_solve_impl(n, indptr, indices, k_vals, nnz, nseg, seg_row, ncol, b, x, rtol, maxiter, 1, inner_rtol,
+                        status_out, relres_out, iters_out, ws, ws_bytes, (cudaStream_t)stream, &pc);
 }
 
 // ---------------------------------------------------------------------------
