@@ -47,27 +47,12 @@ K_EIG = 50
 
 # ----------------------------------------------------------------------------- workload
 def make_batch(n_meshes: int, seed: int, levels=(3, 4, 5, 6)):
-    """Deterministic deformed icospheres; the SH basis is evaluated once per level."""
-    from lapy_gb300 import TriaMesh, meshes
+    """Deterministic deformed icospheres (per-mesh seed), level uniform in ``levels``."""
+    from lapy_gb300 import meshes
 
     rng = np.random.default_rng(seed)
     lv = rng.choice(levels, size=n_meshes)
-    base = {L: meshes.icosphere(int(L)) for L in sorted(set(lv.tolist()))}
-    basis = {}
-    for L, m in base.items():
-        u = m.v / np.linalg.norm(m.v, axis=1, keepdims=True)
-        th = np.arccos(np.clip(u[:, 2], -1, 1))
-        ph = np.arctan2(u[:, 1], u[:, 0])
-        basis[L] = (u, np.stack([meshes.real_sph_harm(l, mm, th, ph) for l in range(9) for mm in range(-l, l + 1)],
-                                axis=1))
-    out = []
-    scale = np.array([1.0 / (1 + l) for l in range(9) for _ in range(2 * l + 1)])
-    for i, L in enumerate(lv.tolist()):
-        c = np.random.default_rng(seed * 100003 + i).standard_normal(81) * scale
-        u, Y = basis[L]
-        r = 1.0 + 0.1 * (Y @ c)
-        out.append(TriaMesh(u * r[:, None], base[L].t))
-    return out, lv
+    return meshes.deformed_icospheres(lv.tolist(), [seed * 100003 + i for i in range(n_meshes)]), lv
 
 
 def rank_seed(seed: int, rank: int) -> int:
@@ -294,6 +279,8 @@ def run_gpu(args, rank, world):
         line["heat"] = run_heat(args, meshes, lv, batch_in, world)
     if not args.no_plain:
         line["plain"] = run_plain_spectra(args, meshes, lv, line["value"] / world)
+    if not args.no_learned:
+        line["learned"] = run_learned(args)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"], heat_cpu = cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
         if "heat" in line:
@@ -361,6 +348,17 @@ def run_heat(args, meshes, lv, batch_in, world):
             "vs_plain": value / (world * plain)}
 
 
+def run_learned(args):
+    """Learned SPAI: training on 4,096 level-6 systems, then Jacobi-PCG against
+    learned-SPAI-PCG on held-out level-7 meshes (rel. residual 1e-8)."""
+    from lapy_gb300 import spai_train
+
+    net, hist = spai_train.train(n_meshes=128, level=6, systems=4096, batch=32, seed=args.seed)
+    ev = spai_train.evaluate(net, n_test=args.learned_test, level=7, seed=args.seed + 1)
+    return {"train": hist, "test": ev,
+            "note": "factored SPAI G'G (per-edge MLP, BF16 weights) vs Jacobi; same PCG, same tolerance"}
+
+
 def run_plain_spectra(args, meshes, lv, batched_per_gpu):
     """The unbatched GPU method: Solver(mesh).eigs(50) one mesh at a time."""
     import torch
@@ -368,19 +366,19 @@ def run_plain_spectra(args, meshes, lv, batched_per_gpu):
     from lapy_gb300 import Solver
 
     idx = stratified(lv, args.plain_per_level)
-    Solver(meshes[idx[0]]).eigs(k=K_EIG)  # warm
+    Solver(meshes[idx[0]]).eigs(k=K_EIG, precond="jacobi")  # warm
     secs = []
     for i in idx:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        Solver(meshes[i]).eigs(k=K_EIG)
+        Solver(meshes[i]).eigs(k=K_EIG, precond="jacobi")
         torch.cuda.synchronize()
         secs.append(time.perf_counter() - t0)
     total, by_level = extrapolate(lv, idx, secs)
     plain = args.meshes / total
     return {"value": plain, "unit": "spectra/s", "per_gpu": True,
-            "sample": f"{len(idx)} meshes ({args.plain_per_level} per level) through Solver(mesh).eigs(50) one at a "
-                      f"time (Jacobi-PCG), extrapolated by level counts", "sec_per_mesh_by_level": by_level,
+            "sample": f"{len(idx)} meshes ({args.plain_per_level} per level) through Solver(mesh).eigs(50, "
+                      f"precond='jacobi') one at a time, extrapolated by level counts", "sec_per_mesh_by_level": by_level,
             "vs_plain": batched_per_gpu / plain}
 
 
@@ -415,13 +413,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--meshes", type=int, default=512)
-    ap.add_argument("--block", type=int, default=2)
+    ap.add_argument("--block", type=int, default=4)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-per-level", type=int, default=4)
     ap.add_argument("--plain-per-level", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-heat", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-test", type=int, default=32, help="held-out level-7 meshes of the learned-SPAI leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the public-API end-to-end leg (profiling runs)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))

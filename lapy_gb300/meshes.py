@@ -78,6 +78,29 @@ def sh_deform(mesh: TriaMesh, seed: int, lmax: int = 8, amp: float = 0.1) -> Tri
     return TriaMesh(u * r[:, None], mesh.t.copy())
 
 
+def deformed_icospheres(levels, seeds, lmax: int = 8, amp: float = 0.1) -> list:
+    """``sh_deform(icosphere(level), seed)`` for many meshes, with the icosphere
+    and its spherical-harmonic basis built once per level."""
+    base, basis = {}, {}
+    out = []
+    for level, seed in zip(levels, seeds):
+        level = int(level)
+        if level not in base:
+            m = icosphere(level)
+            u = m.v / np.linalg.norm(m.v, axis=1, keepdims=True)
+            th = np.arccos(np.clip(u[:, 2], -1.0, 1.0))
+            ph = np.arctan2(u[:, 1], u[:, 0])
+            base[level] = (m, u)
+            basis[level] = np.stack([real_sph_harm(l, mm, th, ph) for l in range(lmax + 1)
+                                     for mm in range(-l, l + 1)], axis=1)
+        m, u = base[level]
+        scale = np.array([1.0 / (1 + l) for l in range(lmax + 1) for _ in range(2 * l + 1)])
+        c = np.random.default_rng(int(seed)).standard_normal(len(scale)) * scale
+        r = 1.0 + amp * (basis[level] @ c)
+        out.append(TriaMesh(u * r[:, None], m.t.copy()))
+    return out
+
+
 def kuhn_cube(n: int, jitter: float = 0.0, seed: int = 0) -> TetMesh:
     """Unit cube, n^3 cells x 6 Kuhn tetrahedra; vertex (i,j,k) has index i + (n+1)(j + (n+1)k)."""
     h = 1.0 / n
