@@ -382,6 +382,131 @@ def run_plain_spectra(args, meshes, lv, batched_per_gpu):
             "vs_plain": batched_per_gpu / plain}
 
 
+# ----------------------------------------------------------------------------- single-mesh configurations
+def _single_mesh(args):
+    from lapy_gb300 import meshes
+
+    if args.workload == "c1":
+        return meshes.icosphere(5)
+    if args.workload == "c2":
+        return meshes.kuhn_cube(64, jitter=0.2, seed=args.seed)
+    return meshes.deformed_icospheres([8], [args.seed])[0]
+
+
+def _c2_heat_steps(fem, mesh, steps=10, t=1e-3):
+    """u_{k+1} = (M + t A)^-1 M u_k from the centre vertex (consistent M)."""
+    import torch
+
+    from lapy_gb300 import meshes
+    from lapy_gb300._device import axpby, pcg_solve
+
+    A = fem._A.as_f64()
+    M = fem._M.as_f64()
+    kv = M.on_pattern(A.indptr, A.indices, A.data.numel())
+    axpby(t, A.data.contiguous(), 1.0, kv, out=kv)
+    u = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    u[meshes.kuhn_center_vertex(64)] = 1.0
+    for _ in range(steps):
+        u, _, _ = pcg_solve(A.indptr, A.indices, kv, A.n, kv.numel(), M.matmul(u), 1e-10)
+    return u
+
+
+def _cpu_single(workload, v, t, seed):
+    """The reference method on one host core (oracle: SciPy splu + eigsh)."""
+    import oracle
+
+    t0 = time.perf_counter()
+    if workload == "c1":
+        A, M = oracle.assemble_scipy(v, t)
+        oracle.eigs(A, M, k=50)
+    elif workload == "c2":
+        from scipy.sparse.linalg import splu
+
+        A, M = oracle.assemble_scipy(v, t)
+        oracle.eigs(A, M, k=100)
+        lu = splu((M + 1e-3 * A).tocsc())
+        u = np.zeros(len(v))
+        n = round(len(v) ** (1 / 3)) - 1
+        u[n // 2 + (n + 1) * (n // 2 + (n + 1) * (n // 2))] = 1.0
+        for _ in range(10):
+            u = lu.solve(M @ u)
+    else:
+        u = oracle.diffusion(v, t, 0, m=1.0)
+        oracle.geodesic_f(v, t, u)
+    return time.perf_counter() - t0
+
+
+def cpu_single(workload, mesh, seed, timeout):
+    import multiprocessing as mp
+
+    os.environ.update({"OPENBLAS_NUM_THREADS": "1", "OMP_NUM_THREADS": "1"})
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1) as pool:
+        res = pool.apply_async(_cpu_single, (workload, np.asarray(mesh.v), np.asarray(mesh.t), seed))
+        try:
+            secs = res.get(timeout=timeout)
+        except mp.TimeoutError:
+            pool.terminate()
+            return {"value": None, "unit": "runs/s", "cores": 1, "kind": "port",
+                    "sample": f"one run of the reference method did not finish within {timeout:.0f} s"}
+    return {"value": 1.0 / secs, "unit": "runs/s", "cores": 1, "kind": "port", "seconds": secs,
+            "sample": "one full run of the reference method (SciPy splu + eigsh / splu solves), one core"}
+
+
+def run_single(args):
+    """C1 (icosphere L5, eigs 50), C2 (Kuhn 64^3 tets: eigs 100 + 10 heat steps),
+    C3 (deformed icosphere L8: heat + heat-method geodesics), from host arrays
+    through the public API each step (so value and e2e coincide)."""
+    import torch
+
+    from lapy_gb300 import Solver, TetMesh, TriaMesh, diffgeo, heat
+
+    mesh0 = _single_mesh(args)
+    cls = TetMesh if args.workload == "c2" else TriaMesh
+    info = {}
+
+    def step():
+        mesh = cls(mesh0.v.copy(), mesh0.t.copy())  # fresh upload every step
+        if args.workload == "c1":
+            ev, _ = Solver(mesh, lump=False).eigs(k=50)
+            info["ev"] = ev
+        elif args.workload == "c2":
+            fem = Solver(mesh, lump=False)
+            ev, _ = fem.eigs(k=100)
+            u = _c2_heat_steps(fem, mesh)
+            info["ev"] = ev
+            info["u_sum"] = float(u.sum())
+        else:
+            u = heat.diffusion(mesh, 0, m=1.0)
+            d = diffgeo.compute_geodesic_f(mesh, u)
+            info["dmax"] = float(np.max(d))
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        wall = time.perf_counter() - t0
+    names = {"c1": ("k=50 spectra/s (icosphere L5, 10,242 vertices)", "spectra/s"),
+             "c2": ("C2 runs/s (Kuhn 64^3 tets: eigs(100) + 10 heat steps)", "runs/s"),
+             "c3": ("C3 runs/s (deformed icosphere L8: heat + geodesics)", "runs/s")}
+    metric, unit = names[args.workload]
+    v = args.steps / wall
+    line = {"metric": metric, "value": v, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 inner PCG / f64 Lanczos and refinement", "data": "synthetic",
+            "config": {"workload": args.workload, "vertices": int(len(mesh0.v)), "elements": int(len(mesh0.t))},
+            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": int(mesh0.v.nbytes + mesh0.t.size * 4),
+                    "d2h_bytes_per_step": int(8 * (50 if args.workload == "c1" else len(mesh0.v)))},
+            "clocks": clk.summary(), "check": {k: (float(np.asarray(x).ravel()[-1]) if k == "ev" else x)
+                                               for k, x in info.items()}}
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_single(args.workload, mesh0, args.seed, args.cpu_timeout)
+    return line
+
+
 def run_reference(args):
     meshes, lv = make_batch(args.meshes, seed=args.seed)
     vals = []
@@ -412,12 +537,15 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="shapedna", choices=["shapedna", "c1", "c2", "c3"],
+                    help="shapedna: the batched headline (512 meshes); c1-c3: single-mesh configurations")
     ap.add_argument("--meshes", type=int, default=512)
     ap.add_argument("--block", type=int, default=4)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-per-level", type=int, default=4)
     ap.add_argument("--plain-per-level", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-timeout", type=float, default=600.0, help="single-mesh workloads: CPU run time limit (s)")
     ap.add_argument("--no-heat", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
@@ -429,6 +557,10 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.workload != "shapedna":
+        if rank == 0:
+            print(json.dumps(run_single(args)), flush=True)
         return
     if world > 1:
         import torch

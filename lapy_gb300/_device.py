@@ -240,6 +240,14 @@ class DeviceCSR:
         return y
 
 
+def axpby(a: float, x: torch.Tensor, b: float, y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """out = a x + b y element-wise on the device (float64; out may alias y)."""
+    out = torch.empty_like(y) if out is None else out
+    _lib.check(_lib.lib().lapy_vec_axpby(y.numel(), float(a), dptr(x), float(b), dptr(y), dptr(out), stream()),
+               "vec_axpby")
+    return out
+
+
 def pcg_solve(indptr, indices, k_vals, n, nnz, b: torch.Tensor, rtol: float, maxiter: int = 20000,
               mixed: bool = True, inner_rtol: float = 1e-4, seg_row=None):
     """Solve K X = B on the device (B: n or n x F float64); returns (X, relres, iters)."""

@@ -18,7 +18,17 @@ namespace lapy {
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-static int64_t seg_cap(int64_t rows) { return rows <= 0 ? 0 : (rows + kAggMinAvg - 1) / kAggMinAvg; }
+// Aggregate size for a segment of `rows` rows: kAggTarget, grown for large
+// segments so that the coarse dimension stays below about 0.8 kCoarseMaxDim.
+static int seg_target(int64_t rows) {
+  return (int)std::max<int64_t>(kAggTarget, (rows * 5 + 4 * kCoarseMaxDim - 1) / (4 * kCoarseMaxDim));
+}
+// Largest accepted coarse dimension: aggregates average at least 5/8 of the target.
+static int64_t seg_cap(int64_t rows) {
+  if (rows <= 0) return 0;
+  const int64_t min_avg = std::max<int64_t>(1, (int64_t)seg_target(rows) * kAggMinAvg / kAggTarget);
+  return (rows + min_avg - 1) / min_avg;
+}
 
 int64_t two_level_max_aggs(const int32_t* seg_row, int nseg) {
   int64_t t = 0;
@@ -49,9 +59,10 @@ static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, cons
                              int32_t* lab) {
   const int32_t len = r1 - r0;
   if (len <= 0) return 0;
+  const int target = seg_target(len);
   for (int32_t v = r0; v < r1; ++v) lab[v] = -1;
   std::vector<int32_t> queue;
-  queue.reserve(kAggTarget);
+  queue.reserve(target);
   int32_t id = 0;
   for (int32_t v = r0; v < r1; ++v) {
     if (lab[v] >= 0) continue;
@@ -59,9 +70,9 @@ static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, cons
     queue.push_back(v);
     lab[v] = id;
     int cnt = 1;
-    for (size_t qi = 0; qi < queue.size() && cnt < kAggTarget; ++qi) {
+    for (size_t qi = 0; qi < queue.size() && cnt < target; ++qi) {
       const int32_t u = queue[qi];
-      for (int32_t k = indptr[u]; k < indptr[u + 1] && cnt < kAggTarget; ++k) {
+      for (int32_t k = indptr[u]; k < indptr[u + 1] && cnt < target; ++k) {
         const int32_t w = indices[k];
         if (w < r0 || w >= r1 || lab[w] >= 0) continue;
         lab[w] = id;
@@ -71,7 +82,7 @@ static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, cons
     }
     ++id;
   }
-  // merge aggregates below kAggTarget / 4 rows into the neighbour aggregate
+  // merge aggregates below target / 4 rows into the neighbour aggregate
   // with the most connecting entries (ties: the smaller id)
   std::vector<std::vector<int32_t>> members(id);
   for (int32_t v = r0; v < r1; ++v) members[lab[v]].push_back(v);
@@ -84,7 +95,7 @@ static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, cons
   std::vector<int32_t> conn_ids;
   std::vector<int32_t> conn_cnt;
   for (int32_t a = 0; a < id; ++a) {
-    if (parent[a] != a || (int)members[a].size() >= kAggTarget / 4) continue;
+    if (parent[a] != a || (int)members[a].size() >= target / 4) continue;
     conn_ids.clear();
     conn_cnt.clear();
     for (int32_t u : members[a]) {

@@ -5,10 +5,12 @@
 namespace lapy {
 
 // Aggregates are grown by breadth-first search on the matrix graph of each
-// segment up to kAggTarget rows; aggregates below kAggTarget / 4 rows are
-// merged into their most strongly connected neighbour.  A segment whose
-// aggregation gives more than ceil(rows / kAggMinAvg) aggregates gets no
-// coarse space (its preconditioner stays Jacobi).
+// segment up to a target size (kAggTarget rows, grown for segments above
+// 0.8 kCoarseMaxDim * kAggTarget rows so the coarse dimension stays bounded);
+// aggregates below a quarter of the target are merged into their most
+// strongly connected neighbour.  A segment whose aggregates average fewer
+// than kAggMinAvg / kAggTarget of the target gets no coarse space (its
+// preconditioner stays Jacobi).
 constexpr int kAggTarget = 64;
 constexpr int kAggMinAvg = 40;
 // Largest coarse dimension per segment that the dense inverse handles.

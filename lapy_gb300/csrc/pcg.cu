@@ -415,6 +415,55 @@ __device__ __forceinline__ void apply_diag_coarse(const PcgArgs<V>& a, int row, 
   }
 }
 
+// Row `row` of Mat * Xin for the calling lane (unit u, lane = row): from the
+// SELL copy when present, else the CSR arrays.  No warp synchronisation: lanes
+// of rows past the unit's end may call it and ignore the result.
+template <typename V, int NP>
+__device__ __forceinline__ void row_apply(const SellMatrix<V>& sm, const int32_t* __restrict__ ptr,
+                                          const int32_t* __restrict__ idx, const V* __restrict__ val,
+                                          const V* __restrict__ Xin, int u, int row, bool valid, V (&acc)[NP]) {
+#pragma unroll
+  for (int q = 0; q < NP; ++q) acc[q] = V(0);
+  if (sm.val) {
+    const int lane = threadIdx.x & 31;
+    const int32_t base = sm.slice_ptr[u];
+    const int w = (sm.slice_ptr[u + 1] - base) >> 5;
+#pragma unroll 4
+    for (int k = 0; k < w; ++k) {
+      const V a = __ldg(sm.val + base + 32 * k + lane);
+      V xr[NP];
+      load_row<V, NP>(Xin, __ldg(sm.col + base + 32 * k + lane), xr);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
+    }
+  } else if (valid) {
+    for (int32_t k = ptr[row]; k < ptr[row + 1]; ++k) {
+      const V a = val[k];
+      V xr[NP];
+      load_row<V, NP>(Xin, idx[k], xr);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
+    }
+  }
+}
+
+// T = G R on the piece's rows; returns the partial ||T||^2 (= r' G'G r) per column.
+template <typename V, int NP>
+__device__ __forceinline__ void factor_first_half(const PcgArgs<V>& a, int u0, int u1, ScalarOf<V> (&acc)[NP]) {
+  const int lane = threadIdx.x & 31;
+  for (int u = u0; u < u1; ++u) {
+    const int row = a.unit_row[u] + lane;
+    const bool valid = row < a.unit_row[u + 1];
+    V t[NP];
+    row_apply<V, NP>(a.pc.g_sell, a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, u, row, valid, t);
+    if (valid) {
+      store_row<V, NP>(a.T, row, t);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] += t[q] * t[q];
+    }
+  }
+}
+
 // Loop over this warp's pieces: s = segment, [u0, u1) = units of the piece.
 #define FOR_MY_PIECES(a, ...)                                                               \
   for (int vw = gw; vw < (a).nvw; vw += nw) {                                                \
@@ -481,28 +530,28 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
     if (!grid_sync(a.bar)) return;
     coarse_solve<V, NP>(a, nullptr, true, gw, nw);
   }
-  if (PC == kPrecFactored) {
-    S dummy[NP];
-    if (!grid_sync(a.bar)) return;
-    FOR_MY_PIECES(a, {
-      for (int u = u0; u < u1; ++u)
-        unit_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.unit_row[u],
-                                a.unit_row[u + 1], wval, widx, dummy);
-    })
+  if constexpr (PC == kPrecFactored) {  // r'z = ||G r||^2; P = G'(G r) below
     if (!grid_sync(a.bar)) return;
     FOR_MY_PIECES(a, {
       S acc[NP];
 #pragma unroll
       for (int q = 0; q < NP; ++q) acc[q] = S(0);
-      for (int u = u0; u < u1; ++u)
-        unit_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.P, a.R, a.unit_row[u],
-                               a.unit_row[u + 1], wval, widx, acc);
+      factor_first_half<V, NP>(a, u0, u1, acc);
       warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
     })
   }
   if (!grid_sync(a.bar)) return;
   // ---- segment initialisation (the warp holding a segment's first piece publishes)
   FOR_MY_PIECES(a, {
+    if constexpr (PC == kPrecFactored) {
+      for (int u = u0; u < u1; ++u) {
+        const int row = a.unit_row[u] + lane;
+        const bool valid = row < a.unit_row[u + 1];
+        V z[NP];
+        row_apply<V, NP>(a.pc.gt_sell, a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, u, row, valid, z);
+        if (valid) store_row<V, NP>(a.P, row, z);
+      }
+    }
     if constexpr (PC == kPrecTwoLevel) {
       for (int u = u0; u < u1; ++u) {
         const int row = a.unit_row[u] + lane;
@@ -753,22 +802,16 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
       if (!grid_sync(a.bar)) return;
     }
 
-    if (PC == kPrecFactored) {
-      // ---- phase B2: T = G R ; phase B3: Z = Gt T, partial r'z
-      S dummy[NP];
-      FOR_MY_PIECES(a, {
-        for (int u = u0; u < u1; ++u)
-          unit_spmm<V, NP, false>(a.pc.g_ptr, a.pc.g_idx, a.pc.g_val, a.R, a.T, nullptr, a.unit_row[u],
-                                  a.unit_row[u + 1], wval, widx, dummy);
-      })
-      if (!grid_sync(a.bar)) return;
+    if constexpr (PC == kPrecFactored) {
+      // ---- phase B2: T = G R and r'z = ||T||^2 (G'T is applied in phase C)
       FOR_MY_PIECES(a, {
         S acc[NP];
 #pragma unroll
         for (int q = 0; q < NP; ++q) acc[q] = S(0);
-        for (int u = u0; u < u1; ++u)
-          unit_spmm<V, NP, true>(a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, a.Z, a.R, a.unit_row[u],
-                                 a.unit_row[u + 1], wval, widx, acc);
+        bool anyact = false;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) anyact |= st_cur[s * NP + q] == kActive;
+        if (anyact) factor_first_half<V, NP>(a, u0, u1, acc);
         warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
       })
       if (!grid_sync(a.bar)) return;
@@ -831,7 +874,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
               load_row<V, NP>(a.R, row, r);
               apply_diag_coarse<V, NP, PC>(a, row, r, z);
             } else {
-              load_row<V, NP>(a.Z, row, z);
+              row_apply<V, NP>(a.pc.gt_sell, a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, u, row, true, z);
             }
             load_row<V, NP>(a.P, row, pv);
 #pragma unroll
@@ -910,8 +953,8 @@ __global__ void sell_fill_kernel(int nunit, const int32_t* __restrict__ unit_row
   }
 }
 
-size_t sell_bytes_bound(int64_t nnz, const ChunkTable& ct, int elem_size) {
-  const size_t elems = (size_t)(1.5 * (double)nnz) + 64 * (size_t)ct.nunit;
+size_t sell_bytes_bound(int64_t nnz, const ChunkTable& ct, int elem_size, double pad) {
+  const size_t elems = (size_t)(pad * (double)nnz) + 64 * (size_t)ct.nunit;
   return a256(4 * (size_t)(ct.nunit + 1)) + a256(4 * (size_t)scan_scratch_elems(ct.nunit + 1)) +
          a256(4 * (size_t)(ct.nunit + 1)) + a256(4 * elems) + a256((size_t)elem_size * elems) + 256;
 }
@@ -954,7 +997,7 @@ template int build_sell<double>(int64_t, const int32_t*, const int32_t*, const d
 
 size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond, int64_t nagg) {
   const size_t vec = a256((size_t)n * p * elem_size);
-  size_t b = vec * (precond == kPrecFactored ? 5 : 3);  // R P Q (+ Z T)
+  size_t b = vec * (precond == kPrecFactored ? 4 : 3);  // R P Q (+ T)
   b += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
   b += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
   b += a256(sizeof(double) * (size_t)ct.nseg * p);
@@ -1032,7 +1075,6 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.Z = nullptr;
   a.T = nullptr;
   if (pc.kind == kPrecFactored) {
-    a.Z = (V*)w; w += vec;
     a.T = (V*)w; w += vec;
   }
   using S = ScalarOf<V>;

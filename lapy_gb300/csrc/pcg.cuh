@@ -55,8 +55,9 @@ struct SellMatrix {
   const V* val = nullptr;
 };
 // Workspace reserved for a SELL copy: values and columns for up to
-// 1.5 nnz + 64 entries per unit (mesh matrices pad by a few percent).
-size_t sell_bytes_bound(int64_t nnz, const ChunkTable& ct, int elem_size);
+// pad * nnz + 64 entries per unit (full mesh matrices pad by a few percent;
+// the triangular halves of a factor pad much more: their row lengths vary).
+size_t sell_bytes_bound(int64_t nnz, const ChunkTable& ct, int elem_size, double pad = 1.5);
 // Build the SELL copy into `mem`; *fits = false (and no copy) when the padded
 // matrix exceeds the reserved space.
 template <typename V>
@@ -78,6 +79,7 @@ struct PcgPrecondDesc {
   const int32_t* gt_ptr = nullptr;
   const int32_t* gt_idx = nullptr;
   const V* gt_val = nullptr;
+  SellMatrix<V> g_sell, gt_sell;      // optional SELL copies of G and G' (val == nullptr: CSR)
   int nagg = 0;                       // aggregates over all segments
   const int32_t* agg = nullptr;       // n: aggregate of each row (-1: none)
   const int32_t* agg_ptr = nullptr;   // nagg + 1: member rows of each aggregate

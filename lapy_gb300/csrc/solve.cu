@@ -291,6 +291,19 @@ extern "C" size_t lapy_pcg_solve_workspace_bytes(int64_t n, int64_t nnz, int nse
                       nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row);
 }
 
+// Padding allowance of the SELL copies of a triangular factor (slices take the
+// longest row of 32; the lower half of a mesh pattern has rows of 1 to ~8).
+constexpr double kFactorPad = 3.0;
+
+// Two SELL copies (G and G') of the lower / upper halves of an n x n pattern
+// with nnz entries, on the PCG's unit table.
+static size_t factor_sell_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row) {
+  ChunkTable ct;
+  std::vector<int32_t> srow(seg_row, seg_row + nseg + 1);
+  plan_chunks(srow.data(), nseg, 4 * lapy_num_sms(), &ct);
+  return 2 * sell_bytes_bound((nnz + n) / 2, ct, sizeof(float), kFactorPad) + 512;
+}
+
 // Shared body of the PCG entry points; `factored` (may be null) selects the
 // factored preconditioner z = G' (G r) with FP32 factors on CSR patterns.
 static int pcg_solve_impl(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
@@ -308,10 +321,10 @@ static int pcg_solve_impl(int64_t n, const int32_t* indptr, const int32_t* indic
     lapy_set_last_message("pcg_solve: segment rows must span [0, n)");
     return LAPY_ERR_INVALID;
   }
-  if (ws_bytes < solve_layout(n, nnz, nseg, ncol, mixed, precond, nullptr, nullptr, nullptr, nullptr, nullptr,
-                              nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                              seg_row))
-    return LAPY_ERR_WORKSPACE;
+  const size_t main_bytes = solve_layout(n, nnz, nseg, ncol, mixed, precond, nullptr, nullptr, nullptr, nullptr,
+                                         nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                         nullptr, nullptr, seg_row);
+  if (ws_bytes < main_bytes + (factored ? factor_sell_bytes(n, nnz, nseg, seg_row) : 0)) return LAPY_ERR_WORKSPACE;
   int32_t* diag_pos;
   double *dinv64, *Bp, *Xp;
   float *dinv32, *k32;
@@ -335,7 +348,19 @@ static int pcg_solve_impl(int64_t n, const int32_t* indptr, const int32_t* indic
   K.k32 = k32;
   K.dinv64 = dinv64;
   K.dinv32 = dinv32;
-  if (factored) K.pc32 = *factored;
+  if (factored) {
+    // SELL copies of G and G' on the PCG's units (CSR when they do not fit)
+    K.pc32 = *factored;
+    const size_t gsb = sell_bytes_bound((nnz + n) / 2, ct, sizeof(float), kFactorPad);
+    char* gmem = base + a256(main_bytes);
+    bool fits = false;
+    LAPY_TRY(build_sell<float>(n, factored->g_ptr, factored->g_idx, factored->g_val, ct, gmem, gsb, &K.pc32.g_sell,
+                               &fits, stream));
+    if (!fits) K.pc32.g_sell = SellMatrix<float>();
+    LAPY_TRY(build_sell<float>(n, factored->gt_ptr, factored->gt_idx, factored->gt_val, ct, gmem + gsb, gsb,
+                               &K.pc32.gt_sell, &fits, stream));
+    if (!fits) K.pc32.gt_sell = SellMatrix<float>();
+  }
   if (mixed) {
     bool fits = false;
     LAPY_TRY(build_sell<float>(n, indptr, indices, k32, ct, sell_mem, sell_bytes, &K.sell32, &fits, stream));
@@ -376,8 +401,9 @@ extern "C" int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* i
 extern "C" size_t lapy_spai_pcg_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row,
                                                 int ncol) {
   if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0) return 0;
-  return solve_layout(n, nnz, nseg, ncol, 1, kPrecFactored, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                      nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row);
+  return a256(solve_layout(n, nnz, nseg, ncol, 1, kPrecFactored, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                           nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row)) +
+         factor_sell_bytes(n, nnz, nseg, seg_row) + 256;
 }
 
 extern "C" int lapy_spai_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,

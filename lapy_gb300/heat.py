@@ -14,13 +14,21 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._device import dptr, pcg_solve, stream
+from ._device import axpby, dptr, pcg_solve, stream
 
 logger = logging.getLogger(__name__)
 
 
-def diffusion(geometry, vids, m: float = 1.0, aniso=None, use_cholmod: bool = False, rtol: float = 1e-11):
-    """Heat diffusion from the vertices in ``vids`` (same semantics as the reference)."""
+def diffusion(geometry, vids, m: float = 1.0, aniso=None, use_cholmod: bool = False, rtol: float = 1e-11,
+              precond: str = "jacobi"):
+    """Heat diffusion from the vertices in ``vids`` (same semantics as the reference).
+
+    ``precond``: ``"jacobi"`` or ``"learned"`` (the shipped per-edge MLP
+    sparse approximate inverse; isotropic systems only)."""
+    if precond not in ("jacobi", "learned"):
+        raise ValueError(f"precond must be 'jacobi' or 'learned', not {precond!r}")
+    if precond == "learned" and aniso is not None:
+        raise ValueError("the learned preconditioner covers isotropic systems (aniso=None)")
     if use_cholmod:
         from .solver import _import_optional
 
@@ -45,7 +53,7 @@ def diffusion(geometry, vids, m: float = 1.0, aniso=None, use_cholmod: bool = Fa
     # hmat = M + t A on A's pattern (lumped M added to the diagonal)
     L = _lib.lib()
     hvals = fem._M.as_f64().on_pattern(A.indptr, A.indices, A.data.numel())
-    hvals.add_(A.data.double(), alpha=t)
+    axpby(t, A.data.double().contiguous(), 1.0, hvals, out=hvals)
     n_cases = len(vids_list)
     b0 = np.zeros((nv, n_cases))
     for k, v in enumerate(vids_list):
@@ -53,7 +61,14 @@ def diffusion(geometry, vids, m: float = 1.0, aniso=None, use_cholmod: bool = Fa
     if n != nv:
         raise ValueError(f"mesh has {nv} vertices but its elements reference only {n}")
     B = torch.from_numpy(b0).to("cuda")
-    x, relres, iters = pcg_solve(A.indptr, A.indices, hvals, n, hvals.numel(), B, rtol)
+    if precond == "learned":
+        from .shapedna import BatchInput
+        from .spai import SpaiSystems, learned_solve
+
+        sysg = SpaiSystems(BatchInput([geometry]), "heat", t=[t])
+        x, relres, iters = learned_solve(sysg, B, rtol)
+    else:
+        x, relres, iters = pcg_solve(A.indptr, A.indices, hvals, n, hvals.numel(), B, rtol)
     logger.debug("heat solve: %d PCG iterations, max rel. residual %.2e", iters, float(np.max(relres)))
     vfunc = x.cpu().numpy()
     del L
@@ -92,8 +107,9 @@ class HeatBatch:
         self.b0 = torch.from_numpy(b0).to("cuda")
         self.ones = torch.ones(nseg, dtype=torch.float64, device="cuda")
 
-    def solve(self, rtol: float = 1e-11, maxiter: int = 20000):
-        """Assemble and solve every segment; returns (u (n,), info)."""
+    def solve(self, rtol: float = 1e-11, maxiter: int = 20000, precond: str = "jacobi"):
+        """Assemble and solve every segment; returns (u (n,), info).
+        ``precond``: ``"jacobi"`` or ``"learned"`` (per-edge MLP SPAI)."""
         from .shapedna import BatchedFEM
 
         inp = self.input
@@ -110,17 +126,24 @@ class HeatBatch:
         _lib.check(L.lapy_csr_seg_axpby(nseg, dptr(seg_dev), dptr(fem.indptr), dptr(fem.pattern.diag_pos),
                                         dptr(t), dptr(fem.a_vals), dptr(self.ones), dptr(fem.m_vals), 1,
                                         dptr(hvals), stream()), "csr_seg_axpby")
-        x, relres, iters = pcg_solve(fem.indptr, fem.indices, hvals, fem.n, fem.nnz, self.b0, rtol, maxiter,
-                                     seg_row=inp.seg_row)
+        if precond == "learned":
+            from .spai import SpaiSystems, learned_solve
+
+            x, relres, iters = learned_solve(SpaiSystems(inp, "heat", t=t), self.b0, rtol, maxiter)
+        elif precond == "jacobi":
+            x, relres, iters = pcg_solve(fem.indptr, fem.indices, hvals, fem.n, fem.nnz, self.b0, rtol, maxiter,
+                                         seg_row=inp.seg_row)
+        else:
+            raise ValueError(f"precond must be 'jacobi' or 'learned', not {precond!r}")
         return x, {"relres": relres, "iters": iters, "t": t, "avg_edge_length": avg}
 
 
-def diffusion_batch(meshes, vids=0, m: float = 1.0, rtol: float = 1e-11) -> list:
+def diffusion_batch(meshes, vids=0, m: float = 1.0, rtol: float = 1e-11, precond: str = "jacobi") -> list:
     """Heat diffusion on many meshes at once: ``diffusion(mesh_s, vids[s], m)``
     for every mesh, solved as one block-diagonal batch.  ``vids``: one vertex
     per mesh, or one vertex index used for all meshes."""
     hb = HeatBatch(meshes, vids, m)
-    x, _ = hb.solve(rtol)
+    x, _ = hb.solve(rtol, precond=precond)
     u = x.cpu().numpy()
     seg = hb.input.seg_row
     return [u[seg[i]:seg[i + 1]] for i in range(len(seg) - 1)]

@@ -158,8 +158,11 @@ class SpaiSystems:
                    "seg_avg_edge_length")
         k = torch.empty(fem.nnz, **f64)
         if kind == "heat":
-            tt = np.broadcast_to(np.asarray(1e-3 if t is None else t, np.float64), (nseg,)).copy()
-            self.t = torch.from_numpy(tt).to("cuda")
+            if isinstance(t, torch.Tensor):
+                self.t = t.to(device="cuda", dtype=torch.float64).contiguous()
+            else:
+                tt = np.broadcast_to(np.asarray(1e-3 if t is None else t, np.float64), (nseg,)).copy()
+                self.t = torch.from_numpy(tt).to("cuda")
             self.sigma = torch.zeros(nseg, **f64)
             ones = torch.ones(nseg, **f64)
             _lib.check(L.lapy_csr_seg_axpby(nseg, dptr(seg), dptr(fem.indptr), dptr(fem.pattern.diag_pos),
@@ -226,6 +229,24 @@ class SpaiSystems:
         return (X[:, 0] if squeeze else X), relres, int(iters.value)
 
 
+_DEFAULT_NET: SpaiNet | None = None
+
+
+def default_net() -> SpaiNet:
+    """The shipped network (trained by lapy_gb300.spai_train), loaded once."""
+    global _DEFAULT_NET
+    if _DEFAULT_NET is None:
+        _DEFAULT_NET = SpaiNet.load(WEIGHTS_FILE)
+    return _DEFAULT_NET
+
+
+def learned_solve(sys_: SpaiSystems, B: torch.Tensor, rtol: float, maxiter: int = 20000, net: SpaiNet | None = None):
+    """Factor with the network and solve (X, relres, iterations)."""
+    net = net or default_net()
+    g, gt, _, _ = sys_.factor(net.forward(sys_.feat))
+    return sys_.solve(B, g, gt, rtol=rtol, maxiter=maxiter)
+
+
 def train_step(net: SpaiNet, sys_: SpaiSystems, lr: float = 3e-3) -> float:
     """One Adam step on the mean Kaporin loss of a batch; returns the loss
     before the step (mean log q over the batch's rows)."""
@@ -243,4 +264,5 @@ def kaporin_loss(net: SpaiNet | None, sys_: SpaiSystems) -> float:
     return float(sys_.factor(w)[2].mean())
 
 
-__all__ = ["SpaiNet", "SpaiPattern", "SpaiSystems", "train_step", "kaporin_loss", "init_params", "NPARAM"]
+__all__ = ["SpaiNet", "SpaiPattern", "SpaiSystems", "train_step", "kaporin_loss", "init_params", "NPARAM",
+           "default_net", "learned_solve"]

@@ -150,3 +150,21 @@ def test_training_beats_jacobi_on_held_out_meshes(cuda_ok):
             assert itl <= 0.8 * itj, (itl, itj)
         else:
             assert itl <= itj, (itl, itj)
+
+
+def test_learned_heat_matches_oracle(cuda_ok):
+    """heat.diffusion / diffusion_batch with the shipped network: the FP64
+    solution of the reference's system, at the heat bar (M-norm rel <= 1e-8)."""
+    from lapy_gb300 import heat
+
+    ms = _meshes([(3, 21), (4, 22)])
+    vids = [0, 5]
+    batch = heat.diffusion_batch(ms, vids, m=1.0, precond="learned")
+    for mesh, v, ub in zip(ms, vids, batch):
+        ref = oracle.diffusion(mesh.v, mesh.t, v, m=1.0)
+        md = oracle.assemble_scipy(mesh.v, mesh.t, lump=True)[1].diagonal()
+        u = heat.diffusion(mesh, v, m=1.0, precond="learned")
+        for x in (u, ub):
+            assert np.sqrt(np.sum(md * (x - ref) ** 2) / np.sum(md * ref ** 2)) <= 1e-8
+    with pytest.raises(ValueError, match="precond"):
+        heat.diffusion(ms[0], 0, precond="ilu")
