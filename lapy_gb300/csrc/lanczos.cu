@@ -17,6 +17,7 @@
 // with OPinv = splu(A - sigma M).solve): same operator, same sigma, same
 // output convention; ARPACK's implicit restarts are replaced by a full basis
 // and the sparse LU by iterative inner solves.
+#include <chrono>
 #include <cmath>
 #include <vector>
 #include "blas.cuh"
@@ -699,9 +700,19 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   res->status.assign(ns, LAPY_ERR_NOCONV);
   res->nbasis.assign(ns, 0);
   // First check once the basis holds ~2.5 k vectors (shift-invert Lanczos
-  // needs 3-5 k); afterwards the gap to k converged pairs sets the stride.
+  // needs 3-5 k); afterwards the stride is the larger of (a) the gap to k
+  // converged pairs and (b) the stride that balances the measured cost of a
+  // check c against that of a block step s: checking every m steps costs c/m
+  // per step and overshoots convergence by (m-1)/2 steps on average, which is
+  // least at m = sqrt(2 c / s).  Both costs are host wall times of code that
+  // already synchronises (a check reads back the convergence flags, a step
+  // its Cholesky-QR flags), so the tuning adds no synchronisation.
   const int first_check = std::max((keff + p + p - 1) / p, (int)std::ceil(2.5 * k / p));
   int next_check = first_check;
+  using clock = std::chrono::steady_clock;
+  double step_s = 0.0, check_s = 0.0;  // running means
+  int nstep_t = 0, ncheck_t = 0;
+  auto t_prev = clock::now();
   std::vector<int32_t> hnconv(ns);
   int j = 0;
   bool all_done = false;
@@ -744,6 +755,11 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     const int m = (j + 1) * p;
     const bool check = (j + 1 >= next_check) || j + 1 == P.mb;
     LAPY_CUDA_TRY(cudaStreamSynchronize(st));
+    {
+      const auto now = clock::now();
+      step_s += (std::chrono::duration<double>(now - t_prev).count() - step_s) / (++nstep_t);
+      t_prev = now;
+    }
     bool any_fail = false;
     for (int s = 0; s < ns; ++s) any_fail |= (hact[s] && hfail[s]);
     if (check || any_fail) {
@@ -767,7 +783,11 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
         hact[s] = hact2[s];
         all_done &= !hact[s];
       }
-      next_check = j + 1 + std::max(1, (int)std::ceil(0.5 * missing / p));
+      const auto now = clock::now();
+      check_s += (std::chrono::duration<double>(now - t_prev).count() - check_s) / (++ncheck_t);
+      t_prev = now;
+      const int balanced = step_s > 0.0 ? (int)std::lround(std::sqrt(2.0 * check_s / step_s)) : 1;
+      next_check = j + 1 + std::max({1, (int)std::ceil(0.5 * missing / p), balanced});
     }
   }
   res->blocks = j;
