@@ -6,8 +6,8 @@ eigensolve, Poisson and heat solves (SciPy eigsh / splu with the reference's
 arguments), and the heat-method geodesic pieces (lapy/diffgeo.py).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
-``bench.py`` may import this package, and only as the checker or as the timed
-CPU baseline.  The product (``lapy_gb300``) never calls it.
+``bench.py`` may import this package, and only as the reference the results are compared
+with or as the timed CPU baseline.  The product (``lapy_gb300``) never calls it.
 
 Parity is pinned: ``tests/golden/make_golden.py`` runs the reference itself on
 the same inputs and stores its outputs under ``tests/golden/``; the CPU tests

@@ -1,5 +1,5 @@
 """TEST INFRASTRUCTURE ONLY -- CPU restatement of the learned factored sparse
-approximate inverse (per-edge MLP) used as the checker of the CUDA kernels.
+approximate inverse (per-edge MLP) that the CUDA kernels are compared with.
 
 No counterpart exists in the reference (lapy solves with splu); this module
 states the method the CUDA kernels implement so that their features, network

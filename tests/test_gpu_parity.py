@@ -267,7 +267,7 @@ def test_gradient_divergence_geodesic(cuda_ok, name):
     np.testing.assert_allclose(dv, d["div_grad_heat0"], rtol=1e-10, atol=1e-12 * np.abs(dv).max())
     gf = diffgeo.compute_geodesic_f(mesh, d["heat0"])
     mdiag = csr_from(d, "M_lump1").diagonal()
-    # the oracle's consistent Neumann solve is the checker at 1e-8; the
+    # the oracle's consistent Neumann solve is the comparison at 1e-8; the
     # reference's singular LU differs from it by up to 2e-5 on the float32
     # fixture meshes (an inconsistent right-hand side amplified by a near-zero
     # pivot), so the reference's output is met at that level

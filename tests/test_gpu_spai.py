@@ -1,7 +1,7 @@
 """Learned SPAI on the GPU against the CPU oracle (oracle/spai.py): pattern
 split, edge features, network forward (BF16 weights), factor / loss / dL/dw,
 the parameter gradient, and what training buys over Jacobi-PCG on held-out
-meshes (judged by iterations, true residual and the FP64 solution)."""
+meshes (assessed by iterations, true residual and the FP64 solution)."""
 
 from __future__ import annotations
 

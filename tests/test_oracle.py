@@ -74,7 +74,7 @@ def test_eigs_match_reference(name):
             np.testing.assert_allclose(ev, ref, rtol=1e-9, atol=1e-9 * scale)
         # Symmetric meshes (icosphere, cube, square) have exactly degenerate
         # groups that a single-vector Krylov space can miss (even with a seeded
-        # start vector), so the dense solve is the checker there.
+        # start vector), so the dense solve is the comparison there.
         evd, _ = oracle.eigs_dense(A, M, k=k)
         np.testing.assert_allclose(evd, ref, rtol=1e-9, atol=1e-9 * scale)
 
