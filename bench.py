@@ -273,6 +273,7 @@ def run_gpu(args, rank, world):
         "clocks": clk.summary(),
         "status_ok": status_ok,
         "pcg": {k: prof[k] for k in ("pcg_launches", "pcg_iterations", "rows", "nnz")},
+        "lanczos": {"segment_steps": prof["lanczos_segment_steps"], "second_cgs_passes": prof["second_cgs_passes"]},
         "wall_s": wall,
     }
     if not args.no_heat:

@@ -45,7 +45,7 @@ long long lapy_launch_count(void);
 /* PCG profile: when enabled, every persistent PCG launch is timed with CUDA
  * events and its work counted.  lapy_profile_read fills up to n of
  * {pcg_ms, pcg_launches, pcg_iterations, rows_processed, nnz_processed,
- *  algorithmic_bytes}. */
+ *  algorithmic_bytes, lanczos_segment_steps, second_cgs_passes}. */
 void lapy_profile_enable(int on);
 void lapy_profile_reset(void);
 int lapy_profile_read(double* out, int n);

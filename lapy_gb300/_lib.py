@@ -172,7 +172,8 @@ def profile_reset() -> None:
 
 def profile_read() -> dict:
     """PCG profile counters (see include/lapy_gb300.h)."""
-    buf = (_dbl * 6)()
-    lib().lapy_profile_read(buf, 6)
-    keys = ("pcg_ms", "pcg_launches", "pcg_iterations", "rows", "nnz", "algorithmic_bytes")
+    buf = (_dbl * 8)()
+    lib().lapy_profile_read(buf, 8)
+    keys = ("pcg_ms", "pcg_launches", "pcg_iterations", "rows", "nnz", "algorithmic_bytes", "lanczos_segment_steps",
+            "second_cgs_passes")
     return dict(zip(keys, list(buf)))

@@ -2,7 +2,7 @@
 
 namespace lapy {
 
-__global__ void seg_col_norm2_kernel(const double* __restrict__ x, int ncol,
+__global__ void seg_col_norm2_kernel(const double* __restrict__ x, const double* __restrict__ y, int ncol,
                                      const int32_t* __restrict__ seg_row, double* __restrict__ out) {
   __shared__ double sh[32];
   const int s = blockIdx.x;
@@ -10,8 +10,7 @@ __global__ void seg_col_norm2_kernel(const double* __restrict__ x, int ncol,
   for (int c = 0; c < ncol; ++c) {
     double acc = 0.0;
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-      const double v = x[r * ncol + c];
-      acc += v * v;
+      acc += x[r * ncol + c] * y[r * ncol + c];
     }
     acc = block_sum(acc, sh);
     if (threadIdx.x == 0) out[(int64_t)s * ncol + c] = acc;
@@ -19,7 +18,12 @@ __global__ void seg_col_norm2_kernel(const double* __restrict__ x, int ncol,
 }
 
 int seg_col_norm2(const double* x, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream) {
-  seg_col_norm2_kernel<<<ct.nseg, 256, 0, stream>>>(x, ncol, ct.seg_row, out);
+  seg_col_norm2_kernel<<<ct.nseg, 256, 0, stream>>>(x, x, ncol, ct.seg_row, out);
+  return lapy_check_launch("seg_col_norm2_kernel");
+}
+
+int seg_col_dot(const double* x, const double* y, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream) {
+  seg_col_norm2_kernel<<<ct.nseg, 256, 0, stream>>>(x, y, ncol, ct.seg_row, out);
   return lapy_check_launch("seg_col_norm2_kernel");
 }
 

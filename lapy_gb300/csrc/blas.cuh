@@ -7,6 +7,8 @@ namespace lapy {
 
 // out[s*ncol + c] = sum over rows of segment s of x[row*ncol + c]^2 (one CTA per segment)
 int seg_col_norm2(const double* x, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream);
+// out[s*ncol + c] = sum over segment s's rows of x(row, c) * y(row, c)
+int seg_col_dot(const double* x, const double* y, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream);
 // y = (float) x
 int cast_f64_f32(int64_t n, const double* x, float* y, cudaStream_t stream);
 // x64 += (double) d32

@@ -41,7 +41,8 @@ int lapy_num_sms() {
 static std::atomic<long long> g_launches{0};
 static std::mutex g_prof_mu;
 static bool g_prof_on = false;
-// pcg_ms, pcg_solves, pcg_iters, rows, nnz, bytes (algorithmic)
+// pcg_ms, pcg_solves, pcg_iters, rows, nnz, bytes (algorithmic),
+// Lanczos (segment, block step) pairs, of which with a second CGS pass
 static double g_prof[8] = {0};
 
 void lapy_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
@@ -58,6 +59,12 @@ void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long 
   // touched: matrix (value + column index per nonzero, row pointer per row),
   // 11 vector streams of p values and 2 of the Jacobi diagonal
   g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (4 + 11.0 * p * eb + 2.0 * eb);
+}
+
+void lapy_profile_add_reorth(long long steps, long long second_passes) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  g_prof[6] += (double)steps;
+  g_prof[7] += (double)second_passes;
 }
 
 extern "C" long long lapy_launch_count(void) { return g_launches.load(); }

@@ -29,6 +29,7 @@ void lapy_count_launch();
 // PCG profile accumulation (enabled by lapy_profile_enable).
 bool lapy_profile_enabled();
 void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int elem_bytes);
+void lapy_profile_add_reorth(long long steps, long long second_passes);
 
 static inline int lapy_check_launch(const char* what) {
   lapy_count_launch();
