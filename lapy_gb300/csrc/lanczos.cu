@@ -62,6 +62,7 @@ struct BMat {
 };
 
 constexpr int kTile = 16;
+constexpr int kGemmChunkRows = 16384;
 
 // partial[c][a][b] = sum over the chunk's rows of X(row, a) * Y(row, b)
 __global__ void __launch_bounds__(256) gemm_tn_partial_kernel(BMat X, int na, BMat Y, int nb,
@@ -206,6 +207,146 @@ __global__ void __launch_bounds__(256) gemm_nn_blk_kernel(const double* __restri
     double* yr = Y + r * P;
 #pragma unroll
     for (int b = 0; b < P; ++b) yr[b] = (beta == 0.0) ? alpha * acc[b] : beta * yr[b] + alpha * acc[b];
+  }
+}
+
+// ---- double-float basis products --------------------------------------------
+// A double x is held as the float pair (hi, lo), hi = fl32(x), lo = fl32(x - hi)
+// (about 48 significant bits).  A product x*y is formed with the FP32
+// error-free transformations: p = fl(xh*yh) and its exact error by fmaf, plus
+// the cross terms xh*yl + xl*yh; the running sum (sh, sl) takes p by an exact
+// two-sum and the error terms in sl.  Relative error about 2^-44 per product,
+// on FP32 instructions, of which this part issues about 64x more per clock
+// than FP64 ones.  The round-to-nearest intrinsics keep the compiler from
+// contracting the steps into FMAs (which would break the exactness).
+__global__ void to_df_kernel(int64_t m, const double* __restrict__ x, float2* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const double v = x[i];
+  const float h = __double2float_rn(v);
+  y[i] = make_float2(h, __double2float_rn(v - (double)h));
+}
+
+__device__ __forceinline__ float2 df_split(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
+}
+
+// (h, l) += (bh, bl), renormalised; commutative, so a butterfly of these
+// leaves the same sum in every lane
+__device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
+  const float s = __fadd_rn(h, bh);
+  const float v = __fsub_rn(s, h);
+  const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, v)), __fsub_rn(bh, v));
+  const float t = __fadd_rn(__fadd_rn(l, bl), e);
+  h = __fadd_rn(s, t);
+  l = __fsub_rn(t, __fsub_rn(h, s));
+}
+
+__device__ __forceinline__ void df_fma(float2 x, float2 y, float& sh, float& sl) {
+  const float p = __fmul_rn(x.x, y.x);
+  float e = fmaf(x.x, y.x, -p);
+  e = fmaf(x.x, y.y, e);
+  e = fmaf(x.y, y.x, e);
+  const float t = __fadd_rn(sh, p);
+  const float v = __fsub_rn(t, sh);
+  const float r = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, v)), __fsub_rn(p, v));
+  sl = __fadd_rn(sl, __fadd_rn(r, e));
+  sh = t;
+}
+
+// TN with the basis in double-float form (see gemm_tn_blk_kernel for the layout).
+template <int P, int JB>
+__global__ void __launch_bounds__(256) gemm_tn_df_kernel(const float2* __restrict__ X, int64_t bst, int nblk,
+                                                         const double* __restrict__ Y,
+                                                         const int32_t* __restrict__ chunk_row,
+                                                         const int32_t* __restrict__ chunk_seg,
+                                                         const int32_t* __restrict__ active,
+                                                         double* __restrict__ partial) {
+  constexpr int NV = JB * P * P;
+  __shared__ double red[8][NV];
+  const int c = blockIdx.x, j0 = blockIdx.y * JB;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float sh[NV], sl[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) { sh[v] = 0.f; sl[v] = 0.f; }
+  if (!active || active[chunk_seg[c]]) {
+    const int64_t r1 = chunk_row[c + 1];
+    for (int64_t r = chunk_row[c] + threadIdx.x; r < r1; r += blockDim.x) {
+      float2 y[P];
+#pragma unroll
+      for (int b = 0; b < P; ++b) y[b] = df_split(__ldg(Y + r * P + b));
+#pragma unroll
+      for (int jj = 0; jj < JB; ++jj) {
+        if (j0 + jj < nblk) {
+          const float2* xr = X + (int64_t)(j0 + jj) * bst + r * P;
+#pragma unroll
+          for (int a = 0; a < P; ++a) {
+            const float2 x = xr[a];
+#pragma unroll
+            for (int b = 0; b < P; ++b) df_fma(x, y[b], sh[(jj * P + a) * P + b], sl[(jj * P + a) * P + b]);
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {  // warp sum in double-float (FP32 instructions)
+    float h = __fadd_rn(sh[v], sl[v]);
+    float l = __fsub_rn(sl[v], __fsub_rn(h, sh[v]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float bh = __shfl_xor_sync(0xffffffffu, h, o), bl = __shfl_xor_sync(0xffffffffu, l, o);
+      df_add(h, l, bh, bl);
+    }
+    if (lane == 0) red[warp][v] = (double)h + (double)l;
+  }
+  __syncthreads();
+  const int na = nblk * P;
+  for (int v = threadIdx.x; v < NV; v += blockDim.x) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][v];
+    const int jj = v / (P * P), a = (v / P) % P, b = v % P;
+    if (j0 + jj < nblk) partial[((int64_t)c * na + (j0 + jj) * P + a) * P + b] = t;
+  }
+}
+
+// NN with the basis in double-float form: Y(row, b) = beta Y + alpha sum X_j(row, a) H[j*P+a][b].
+template <int P>
+__global__ void __launch_bounds__(256) gemm_nn_df_kernel(const float2* __restrict__ X, int64_t bst, int nblk,
+                                                         const double* __restrict__ H, int64_t h_seg_stride,
+                                                         int ldh, double* __restrict__ Y, double alpha, double beta,
+                                                         const int32_t* __restrict__ chunk_row,
+                                                         const int32_t* __restrict__ chunk_seg,
+                                                         const int32_t* __restrict__ active) {
+  extern __shared__ float2 hdf[];
+  const int c = blockIdx.x;
+  const int s = chunk_seg[c];
+  if (active && !active[s]) return;
+  const double* Hs = H + (int64_t)s * h_seg_stride;
+  for (int i = threadIdx.x; i < nblk * P * P; i += blockDim.x) hdf[i] = df_split(Hs[(int64_t)(i / P) * ldh + (i % P)]);
+  __syncthreads();
+  const int64_t r1 = chunk_row[c + 1];
+  for (int64_t r = chunk_row[c] + threadIdx.x; r < r1; r += blockDim.x) {
+    float sh[P], sl[P];
+#pragma unroll
+    for (int b = 0; b < P; ++b) { sh[b] = 0.f; sl[b] = 0.f; }
+    for (int j = 0; j < nblk; ++j) {
+      const float2* xr = X + (int64_t)j * bst + r * P;
+      const float2* hj = hdf + j * P * P;
+#pragma unroll
+      for (int a = 0; a < P; ++a) {
+        const float2 x = xr[a];
+#pragma unroll
+        for (int b = 0; b < P; ++b) df_fma(x, hj[a * P + b], sh[b], sl[b]);
+      }
+    }
+    double* yr = Y + r * P;
+#pragma unroll
+    for (int b = 0; b < P; ++b) {
+      const double acc = (double)sh[b] + (double)sl[b];
+      yr[b] = (beta == 0.0) ? alpha * acc : beta * yr[b] + alpha * acc;
+    }
   }
 }
 
@@ -474,7 +615,7 @@ struct EigPlan {
 struct EigPtrs {
   void* ct_mem; void* gt_mem;
   int32_t* diag_pos; double* k64; float* k32; double* dinv64; float* dinv32;
-  double* basis; double* Y; double* W; double* MW;
+  double* basis; float2* basis_df; double* Y; double* W; double* MW;
   void* ir_ws; size_t ir_bytes;
   void* sell_mem; size_t sell_bytes;
   void* sell64_mem; void* sellm_mem; size_t sell64_bytes;
@@ -499,7 +640,9 @@ static void plan_eig(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, i
   P->lda = P->mb * p;
   std::vector<int32_t> srow(seg_row, seg_row + nseg + 1);
   plan_chunks(srow.data(), nseg, 4 * lapy_num_sms(), &P->ct);
-  plan_chunks(srow.data(), nseg, 2 * lapy_num_sms(), &P->gt);
+  // basis products: long chunks, so a CTA's register tiles sum many rows
+  // before their one reduction
+  plan_chunks(srow.data(), nseg, 2 * lapy_num_sms(), &P->gt, kGemmChunkRows);
 }
 
 static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
@@ -520,6 +663,7 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.dinv64 = (double*)take(8 * n);
   e.dinv32 = (float*)take(4 * n);
   e.basis = (double*)take(8 * (size_t)(P.mb + 1) * n * p);
+  e.basis_df = (float2*)take(8 * (size_t)(P.mb + 1) * n * p);
   e.Y = (double*)take(8 * n * p);
   e.W = (double*)take(8 * n * p);
   e.MW = (double*)take(8 * n * p);
@@ -616,6 +760,51 @@ struct EigOps {
     dim3 g2(P.nseg, std::max(1u, std::min(64u, lapy_ceil_div((int64_t)na * nb, 256))));
     gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, na, nb, P.gt.seg_chunk, out, out_stride, ldo);
     return lapy_check_launch("gemm_tn_reduce_kernel");
+  }
+  // CGS products against basis blocks 0..nbasis/p-1 from the double-float copy
+  template <int PB, int JB>
+  int gemm_tn_df_p(int nbasis, const double* Y, const int32_t* act) const {
+    const int nblk = nbasis / PB;
+    dim3 grid(P.gt.nchunk, lapy_ceil_div(nblk, JB));
+    gemm_tn_df_kernel<PB, JB><<<grid, 256, 0, st>>>(e.basis_df, P.n * PB, nblk, Y, P.gt.chunk_row, P.gt.chunk_seg,
+                                                    act, e.partial);
+    return lapy_check_launch("gemm_tn_df_kernel");
+  }
+  int cgs_tn(int nbasis, const double* MW, double* out, int64_t out_stride, int ldo, const int32_t* act) const {
+    const int p = P.p;
+    int st_ = LAPY_ERR_INVALID;
+    if (p == 1) st_ = gemm_tn_df_p<1, 16>(nbasis, MW, act);
+    else if (p == 2) st_ = gemm_tn_df_p<2, 8>(nbasis, MW, act);
+    else if (p == 4) st_ = gemm_tn_df_p<4, 2>(nbasis, MW, act);
+    else if (p == 8) st_ = gemm_tn_df_p<8, 1>(nbasis, MW, act);
+    else return gemm_tn(BMat{e.basis, p, P.n * p}, nbasis, BMat{MW, p, 0}, p, out, out_stride, ldo, act);
+    LAPY_TRY(st_);
+    dim3 g2(P.nseg, std::max(1u, std::min(64u, lapy_ceil_div((int64_t)nbasis * p, 256))));
+    gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, nbasis, p, P.gt.seg_chunk, out, out_stride, ldo);
+    return lapy_check_launch("gemm_tn_reduce_kernel");
+  }
+  template <int PB>
+  int gemm_nn_df_p(int nbasis, const double* H, int64_t hs, int ldh, double* W, const int32_t* act) const {
+    const int nblk = nbasis / PB;
+    const size_t smem = sizeof(float2) * (size_t)nblk * PB * PB;
+    gemm_nn_df_kernel<PB><<<P.gt.nchunk, 256, smem, st>>>(e.basis_df, P.n * PB, nblk, H, hs, ldh, W, -1.0, 1.0,
+                                                          P.gt.chunk_row, P.gt.chunk_seg, act);
+    return lapy_check_launch("gemm_nn_df_kernel");
+  }
+  // W -= Q H per segment
+  int cgs_nn(int nbasis, const double* H, int64_t hs, int ldh, double* W, const int32_t* act) const {
+    const int p = P.p;
+    const bool fits = sizeof(float2) * (size_t)nbasis * p <= 48 * 1024;
+    if (fits && p == 1) return gemm_nn_df_p<1>(nbasis, H, hs, ldh, W, act);
+    if (fits && p == 2) return gemm_nn_df_p<2>(nbasis, H, hs, ldh, W, act);
+    if (fits && p == 4) return gemm_nn_df_p<4>(nbasis, H, hs, ldh, W, act);
+    if (fits && p == 8) return gemm_nn_df_p<8>(nbasis, H, hs, ldh, W, act);
+    return gemm_nn(BMat{e.basis, p, P.n * p}, nbasis, H, hs, ldh, W, p, p, -1.0, 1.0, act);
+  }
+  int basis_to_df(int j) const {
+    const int64_t m = P.n * P.p;
+    to_df_kernel<<<lapy_ceil_div(m, 256), 256, 0, st>>>(m, e.basis + (size_t)j * m, e.basis_df + (size_t)j * m);
+    return lapy_check_launch("to_df_kernel");
   }
   template <int PB>
   int gemm_nn_blk(BMat X, int na, const double* H, int64_t hs, int ldh, double* Y, double alpha, double beta,
@@ -726,6 +915,7 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   rand_fill_kernel<<<lapy_ceil_div(n * p, 256), 256, 0, st>>>(n * p, seed, Q0);
   LAPY_TRY(lapy_check_launch("rand_fill_kernel"));
   LAPY_TRY(ops.chol_qr2(Q0));
+  LAPY_TRY(ops.basis_to_df(0));
 
   std::vector<int32_t> hfail(ns);
   res->status.assign(ns, LAPY_ERR_NOCONV);
@@ -771,15 +961,15 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     BMat MWm{e.MW, p, 0};
     LAPY_TRY(ops.apply_M(e.W, e.MW, p));
     LAPY_TRY(seg_col_dot(e.W, e.MW, p, P.ct, e.wn0, st));
-    LAPY_TRY(ops.gemm_tn(Qm, nbasis, MWm, p, e.Hsum, (int64_t)lda * p, p, e.active));
-    LAPY_TRY(ops.gemm_nn(Qm, nbasis, e.Hsum, (int64_t)lda * p, p, e.W, p, p, -1.0, 1.0, e.active));
+    LAPY_TRY(ops.cgs_tn(nbasis, e.MW, e.Hsum, (int64_t)lda * p, p, e.active));
+    LAPY_TRY(ops.cgs_nn(nbasis, e.Hsum, (int64_t)lda * p, p, e.W, e.active));
     LAPY_TRY(ops.apply_M(e.W, e.MW, p));
     LAPY_TRY(seg_col_dot(e.W, e.MW, p, P.ct, e.wn1, st));
     reorth_mask_kernel<<<lapy_ceil_div(ns, 128), 128, 0, st>>>(ns, p, e.wn0, e.wn1, kReorthEta * kReorthEta,
                                                                e.active, e.active2, e.rcnt);
     LAPY_TRY(lapy_check_launch("reorth_mask_kernel"));
-    LAPY_TRY(ops.gemm_tn(Qm, nbasis, MWm, p, e.H, (int64_t)lda * p, p, e.active2));
-    LAPY_TRY(ops.gemm_nn(Qm, nbasis, e.H, (int64_t)lda * p, p, e.W, p, p, -1.0, 1.0, e.active2));
+    LAPY_TRY(ops.cgs_tn(nbasis, e.MW, e.H, (int64_t)lda * p, p, e.active2));
+    LAPY_TRY(ops.cgs_nn(nbasis, e.H, (int64_t)lda * p, p, e.W, e.active2));
     // Hsum += H
     LAPY_TRY(vec_axpby((int64_t)ns * lda * p, 1.0, e.Hsum, 1.0, e.H, e.Hsum, st));
     store_T_kernel<<<ns, 256, 0, st>>>(p, j, e.Hsum, (int64_t)lda * p, e.T, lda, e.active);
@@ -787,6 +977,7 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     // new block
     LAPY_CUDA_TRY(cudaMemcpyAsync(Qn, e.W, 8 * n * p, cudaMemcpyDeviceToDevice, st));
     LAPY_TRY(ops.chol_qr2(Qn));
+    LAPY_TRY(ops.basis_to_df(j + 1));
     LAPY_CUDA_TRY(cudaMemcpyAsync(hfail.data(), e.fail, 4 * ns, cudaMemcpyDeviceToHost, st));
     const int m = (j + 1) * p;
     const bool check = (j + 1 >= next_check) || j + 1 == P.mb;

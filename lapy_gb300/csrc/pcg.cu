@@ -31,10 +31,10 @@ constexpr int kPlanCtasPerSm = 4; // resident CTAs per SM the warp plan assumes
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable* ct) {
+int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable* ct, int max_rows) {
   const int64_t total = seg_row[nseg] - seg_row[0];
   int64_t cr = (total + std::max(1, target_chunks) - 1) / std::max(1, target_chunks);
-  cr = std::max<int64_t>(32, std::min<int64_t>(1024, cr));
+  cr = std::max<int64_t>(32, std::min<int64_t>(std::max(32, max_rows), cr));
   cr = (cr + 31) / 32 * 32;
   ct->nseg = nseg;
   ct->h_seg_row.assign(seg_row, seg_row + nseg + 1);

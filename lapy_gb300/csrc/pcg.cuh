@@ -34,8 +34,8 @@ struct ChunkTable {
 };
 
 // Plan chunks (and the PCG's warp plan) for the given segments (host);
-// returns the chunk count.
-int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable* ct);
+// chunks hold 32..max_rows rows.  Returns the chunk count.
+int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable* ct, int max_rows = 1024);
 // Bytes of device memory the table needs.
 size_t chunk_table_bytes(const ChunkTable& ct);
 // Place the table into `mem` and upload it (synchronous on `stream`).
