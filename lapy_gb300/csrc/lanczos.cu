@@ -227,6 +227,15 @@ __global__ void to_df_kernel(int64_t m, const double* __restrict__ x, float2* __
   y[i] = make_float2(h, __double2float_rn(v - (double)h));
 }
 
+// In place: the 8-byte double becomes its 8-byte float pair.
+__global__ void to_df_inplace_kernel(int64_t m, double* x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const double v = x[i];
+  const float h = __double2float_rn(v);
+  reinterpret_cast<float2*>(x)[i] = make_float2(h, __double2float_rn(v - (double)h));
+}
+
 __device__ __forceinline__ float2 df_split(double v) {
   const float h = __double2float_rn(v);
   return make_float2(h, __double2float_rn(v - (double)h));
@@ -348,6 +357,46 @@ __global__ void __launch_bounds__(256) gemm_nn_df_kernel(const float2* __restric
       yr[b] = (beta == 0.0) ? alpha * acc : beta * yr[b] + alpha * acc;
     }
   }
+}
+
+// Final Rayleigh-Ritz products in double-float (one thread per output entry):
+// Y(row, b) = sum_a Q(row, a) H_s[a][b] with Q the double-float basis (blocks
+// of p columns) and H_s pre-split, ...
+__global__ void __launch_bounds__(256) gemm_nn_dfany_kernel(const float2* __restrict__ X, int p, int64_t bst,
+                                                            int na, const float2* __restrict__ H,
+                                                            int64_t h_seg_stride, int ldh, double* __restrict__ Y,
+                                                            int ldy, int nb, const int32_t* __restrict__ chunk_row,
+                                                            const int32_t* __restrict__ chunk_seg) {
+  const int c = blockIdx.x;
+  const float2* Hs = H + (int64_t)chunk_seg[c] * h_seg_stride;
+  const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
+  const int nblk = na / p;
+  for (int64_t e = r0 * nb + threadIdx.x; e < r1 * nb; e += blockDim.x) {
+    const int64_t row = e / nb;
+    const int b = (int)(e - row * nb);
+    float sh = 0.f, sl = 0.f;
+    for (int j = 0; j < nblk; ++j) {
+      const float2* xr = X + (int64_t)j * bst + row * p;
+      for (int q = 0; q < p; ++q) df_fma(xr[q], Hs[(int64_t)(j * p + q) * ldh + b], sh, sl);
+    }
+    Y[row * ldy + b] = (double)sh + (double)sl;
+  }
+}
+
+// ... and partial[c][a][b] = sum over chunk c's rows of X(row, a) Y(row, b)
+// for row-major double-float X (n x na) and Y (n x nb).
+__global__ void __launch_bounds__(256) gemm_tn_dfany_kernel(const float2* __restrict__ X, int na,
+                                                            const float2* __restrict__ Y, int nb,
+                                                            const int32_t* __restrict__ chunk_row,
+                                                            double* __restrict__ partial) {
+  const int c = blockIdx.x;
+  const int a = blockIdx.y * kTile + threadIdx.x / kTile;
+  const int b = blockIdx.z * kTile + threadIdx.x % kTile;
+  if (a >= na || b >= nb) return;
+  float sh = 0.f, sl = 0.f;
+  const int64_t r1 = chunk_row[c + 1];
+  for (int64_t r = chunk_row[c]; r < r1; ++r) df_fma(X[r * na + a], Y[r * nb + b], sh, sl);
+  partial[((int64_t)c * na + a) * nb + b] = (double)sh + (double)sl;
 }
 
 // Selective second CGS pass: segment s repeats the projection when the first
@@ -615,7 +664,7 @@ struct EigPlan {
 struct EigPtrs {
   void* ct_mem; void* gt_mem;
   int32_t* diag_pos; double* k64; float* k32; double* dinv64; float* dinv32;
-  double* basis; float2* basis_df; double* Y; double* W; double* MW;
+  double* basis; float2* basis_df; double* Y; double* W; double* MW; float2* S_df; float2* X_df;
   void* ir_ws; size_t ir_bytes;
   void* sell_mem; size_t sell_bytes;
   void* sell64_mem; void* sellm_mem; size_t sell64_bytes;
@@ -692,6 +741,8 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.Sfinal = (double*)take(8 * (size_t)ns * lda * keff);
   e.theta_final = (double*)take(8 * (size_t)ns * keff);
   e.X = (double*)take(8 * n * keff);
+  e.X_df = (float2*)take(8 * n * keff);
+  e.S_df = (float2*)take(8 * (size_t)ns * lda * keff);
   e.AX = (double*)take(8 * n * keff);
   e.MX = (double*)take(8 * n * keff);
   e.Ak = (double*)take(8 * (size_t)ns * keff * keff);
@@ -1043,14 +1094,39 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   }
   // X = Q S_final (n x keff): basis blocks 0..j-1 (S rows beyond a segment's m are zero)
   const int nb_used = j * p;
-  BMat Qm{e.basis, p, n * p};
-  LAPY_TRY(ops.gemm_nn(Qm, nb_used, e.Sfinal, (int64_t)lda * keff, keff, e.X, keff, keff, 1.0, 0.0, nullptr));
-  // final Rayleigh-Ritz with the exact A and M
+  auto to_df = [&](const double* x, float2* y, int64_t m) {
+    to_df_kernel<<<lapy_ceil_div(m, 256), 256, 0, st>>>(m, x, y);
+    return lapy_check_launch("to_df_kernel");
+  };
+  LAPY_TRY(to_df(e.Sfinal, e.S_df, (int64_t)ns * lda * keff));
+  gemm_nn_dfany_kernel<<<P.gt.nchunk, 256, 0, st>>>(e.basis_df, p, n * p, nb_used, e.S_df, (int64_t)lda * keff,
+                                                    keff, e.X, keff, keff, P.gt.chunk_row, P.gt.chunk_seg);
+  LAPY_TRY(lapy_check_launch("gemm_nn_dfany_kernel"));
+  // final Rayleigh-Ritz with the exact A and M (projections in double-float;
+  // AX and MX are only read by them, so they are split in place)
   LAPY_TRY(csr_spmm<double>(n, indptr, indices, a_vals, keff, e.X, e.AX, 1.0, 0.0, G, st));
   LAPY_TRY(ops.apply_M(e.X, e.MX, keff));
-  BMat Xm{e.X, keff, 0}, AXm{e.AX, keff, 0}, MXm{e.MX, keff, 0};
-  LAPY_TRY(ops.gemm_tn(Xm, keff, AXm, keff, e.Ak, (int64_t)keff * keff, keff, nullptr));
-  LAPY_TRY(ops.gemm_tn(Xm, keff, MXm, keff, e.Mk, (int64_t)keff * keff, keff, nullptr));
+  LAPY_TRY(to_df(e.X, e.X_df, n * keff));
+  for (double* buf : {e.AX, e.MX}) {
+    to_df_inplace_kernel<<<lapy_ceil_div(n * keff, 256), 256, 0, st>>>(n * keff, buf);
+    LAPY_TRY(lapy_check_launch("to_df_inplace_kernel"));
+  }
+  {
+    dim3 grid(P.gt.nchunk, lapy_ceil_div(keff, kTile), lapy_ceil_div(keff, kTile));
+    dim3 g2(P.nseg, std::max(1u, std::min(64u, lapy_ceil_div((int64_t)keff * keff, 256))));
+    gemm_tn_dfany_kernel<<<grid, 256, 0, st>>>(e.X_df, keff, reinterpret_cast<const float2*>(e.AX), keff,
+                                               P.gt.chunk_row, e.partial);
+    LAPY_TRY(lapy_check_launch("gemm_tn_dfany_kernel"));
+    gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, keff, keff, P.gt.seg_chunk, e.Ak, (int64_t)keff * keff,
+                                              keff);
+    LAPY_TRY(lapy_check_launch("gemm_tn_reduce_kernel"));
+    gemm_tn_dfany_kernel<<<grid, 256, 0, st>>>(e.X_df, keff, reinterpret_cast<const float2*>(e.MX), keff,
+                                               P.gt.chunk_row, e.partial);
+    LAPY_TRY(lapy_check_launch("gemm_tn_dfany_kernel"));
+    gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, keff, keff, P.gt.seg_chunk, e.Mk, (int64_t)keff * keff,
+                                              keff);
+    LAPY_TRY(lapy_check_launch("gemm_tn_reduce_kernel"));
+  }
   rr_prepare_kernel<<<ns, 128, 0, st>>>(keff, e.Ak, e.Mk, e.Cneg, e.fail);
   LAPY_TRY(lapy_check_launch("rr_prepare_kernel"));
   std::vector<int32_t> hk(ns, keff);
