@@ -1191,7 +1191,11 @@ extern "C" int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const in
   EigPtrs e;
   layout_eig(P, (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255)), &e);
   EigResult r;
-  const double round_rtol = 1e-4;
+  // FP32 refinement rounds of 1e-3 (measured on the batched workload: 1e-3 /
+  // 1e-4 / 1e-5 / 2e-3 / 1e-2 per round gave 107 / 101 / 95 / 101 / 99 spectra/s;
+  // tighter rounds spend iterations where FP32 CG stalls, looser ones restart
+  // more often)
+  const double round_rtol = 1e-3;
   LAPY_TRY(eigs_run(P, e, indptr, indices, a_vals, m_vals, m_is_diag, sigma, tol, inner_rtol, round_rtol,
                     inner_maxiter, seed, evals, evecs, (cudaStream_t)stream, &r));
   for (int s = 0; s < nseg; ++s) {
