@@ -27,7 +27,7 @@ constexpr int kPcgThreads = 256;
 constexpr int kWarps = kPcgThreads / 32;
 constexpr int kUnit = 32;
 constexpr int kStageWarp = 384;   // staged nonzeros per warp (values + column indices)
-constexpr int kPlanCtasPerSm = 4; // resident CTAs per SM the warp plan assumes
+constexpr int kPlanCtasPerSm = 5; // resident CTAs per SM the warp plan assumes (48 registers)
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -476,7 +476,7 @@ __device__ __forceinline__ void factor_first_half(const PcgArgs<V>& a, int u0, i
   }
 
 template <typename V, int NP, int PC, bool RU>
-__global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<V> a) {
+__global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArgs<V> a) {
   using S = ScalarOf<V>;
   __shared__ V sval_all[kWarps * kStageWarp];
   __shared__ int32_t sidx_all[kWarps * kStageWarp];
