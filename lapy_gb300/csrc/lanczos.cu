@@ -17,7 +17,6 @@
 // with OPinv = splu(A - sigma M).solve): same operator, same sigma, same
 // output convention; ARPACK's implicit restarts are replaced by a full basis
 // and the sparse LU by iterative inner solves.
-#include <chrono>
 #include <cmath>
 #include <vector>
 #include "blas.cuh"
@@ -896,6 +895,15 @@ struct EigOps {
   }
 };
 
+// Cost model of the convergence-check stride (seconds on this part): a dense
+// eigensolve of an m x m projected matrix per CTA, in waves of one CTA per SM;
+// a block step's fixed cost plus its PCG iterations (grid-barrier latency and
+// rows streamed).
+constexpr double kCheckSecPerCube = 2.0e-9;
+constexpr double kStepSec = 1.0e-3;
+constexpr double kIterSec = 2.0e-5;
+constexpr double kIterSecPerRow = 9.0e-11;
+
 // Threshold of the selective second Gram-Schmidt pass (reorth_mask_kernel):
 // the classical 1/sqrt(2).  On the batched ShapeDNA workload about 98 % of the
 // (mesh, block step) pairs still repeat the pass; a threshold of 1e-2 skipped
@@ -973,18 +981,16 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   res->nbasis.assign(ns, 0);
   // First check once the basis holds ~2.5 k vectors (shift-invert Lanczos
   // needs 3-5 k); afterwards the stride is the larger of (a) the gap to k
-  // converged pairs and (b) the stride that balances the measured cost of a
-  // check c against that of a block step s: checking every m steps costs c/m
-  // per step and overshoots convergence by (m-1)/2 steps on average, which is
-  // least at m = sqrt(2 c / s).  Both costs are host wall times of code that
-  // already synchronises (a check reads back the convergence flags, a step
-  // its Cholesky-QR flags), so the tuning adds no synchronisation.
+  // converged pairs and (b) the stride that balances the cost of a check c
+  // against that of a block step s: checking every m steps costs c/m per step
+  // and overshoots convergence by (m-1)/2 steps on average, least at
+  // m = sqrt(2 c / s).  c and s come from a cost model of this GPU (fitted
+  // to measured dense-eigensolver and PCG times), not from timers, so the
+  // stopping step - and with it every result - is the same on every run.
   const int first_check = std::max((keff + p + p - 1) / p, (int)std::ceil(2.5 * k / p));
   int next_check = first_check;
-  using clock = std::chrono::steady_clock;
-  double step_s = 0.0, check_s = 0.0;  // running means
-  int nstep_t = 0, ncheck_t = 0;
-  auto t_prev = clock::now();
+  int64_t step_pcg_iters = 0;
+  const int sms = lapy_num_sms();
   std::vector<int32_t> hnconv(ns);
   int j = 0;
   bool all_done = false;
@@ -1000,6 +1006,7 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     LAPY_TRY(ir_solve(K, P.ct, p, e.Y, e.W, inner_rtol, inner_maxiter, 1, round_rtol, 16, e.ir_ws, e.ir_bytes,
                       st, &irs, nullptr, nullptr));
     res->inner_iters += irs.pcg_iters;
+    step_pcg_iters = irs.pcg_iters;
     if (irs.status == LAPY_ERR_NAN || irs.status == LAPY_ERR_BREAKDOWN) {
       lapy_set_last_message("eigs: inner solve failed (%s)", lapy_status_string(irs.status));
       return irs.status;
@@ -1033,11 +1040,6 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     const int m = (j + 1) * p;
     const bool check = (j + 1 >= next_check) || j + 1 == P.mb;
     LAPY_CUDA_TRY(cudaStreamSynchronize(st));
-    {
-      const auto now = clock::now();
-      step_s += (std::chrono::duration<double>(now - t_prev).count() - step_s) / (++nstep_t);
-      t_prev = now;
-    }
     bool any_fail = false;
     for (int s = 0; s < ns; ++s) any_fail |= (hact[s] && hfail[s]);
     if (check || any_fail) {
@@ -1061,10 +1063,12 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
         hact[s] = hact2[s];
         all_done &= !hact[s];
       }
-      const auto now = clock::now();
-      check_s += (std::chrono::duration<double>(now - t_prev).count() - check_s) / (++ncheck_t);
-      t_prev = now;
-      const int balanced = step_s > 0.0 ? (int)std::lround(std::sqrt(2.0 * check_s / step_s)) : 1;
+      int nact = 0;
+      for (int s = 0; s < ns; ++s) nact += hact[s] != 0;
+      const double mm = (double)(m + p);
+      const double check_cost = kCheckSecPerCube * mm * mm * mm * (double)((nact + sms - 1) / sms);
+      const double step_cost = kStepSec + (double)step_pcg_iters * (kIterSec + kIterSecPerRow * (double)n);
+      const int balanced = (int)std::lround(std::sqrt(2.0 * check_cost / step_cost));
       next_check = j + 1 + std::max({1, (int)std::ceil(0.5 * missing / p), balanced});
     }
   }
