@@ -1,12 +1,17 @@
 // Batched symmetric eigensolver for the small projected matrices of the
 // Lanczos iteration, FP64 throughout, one CTA per matrix:
 //   1. Householder reduction to tridiagonal form (Golub & Van Loan, Alg. 8.3.1),
-//   2. bisection on Sturm sequence counts for the wanted eigenvalues
-//      (Barth, Martin & Wilkinson 1967),
-//   3. inverse iteration on the tridiagonal with partial pivoting, with
-//      modified Gram-Schmidt inside clusters of (near-)equal eigenvalues
-//      (Peters & Wilkinson 1971),
+//   2. multisection on Sturm sequence counts for the wanted eigenvalues
+//      (Barth, Martin & Wilkinson 1967), several lanes per eigenvalue, with a
+//      division-free count,
+//   3. inverse iteration on the tridiagonal with partial pivoting (Peters &
+//      Wilkinson 1971), all eigenvalues at once with the LU factors reused
+//      across sweeps, and modified Gram-Schmidt inside clusters of
+//      (near-)equal eigenvalues after every sweep,
 //   4. back-transformation by the stored Householder reflectors.
+// FP64 throughput is low on this GPU, so the sequential parts (counts,
+// triangular solves) are arranged to issue as few FP64 instructions as
+// possible and to keep every warp of the CTA busy.
 #include <cfloat>
 #include <cmath>
 #include "dense.cuh"
@@ -16,55 +21,102 @@ namespace lapy {
 constexpr int kEigThreads = 256;
 
 size_t sym_eig_work_doubles(int lda, int want) {
-  return (size_t)lda * 6 + (size_t)want * 2 + (size_t)want * 6 * lda + 64;
+  return (size_t)lda * 4 + (size_t)want * 2 + (size_t)want * 5 * lda + 64;
 }
 
-__device__ __forceinline__ int sturm_count(const double* d, const double* e2, int n, double x,
-                                           double pivmin) {
-  int cnt = 0;
-  double q = d[0] - x;
-  if (fabs(q) < pivmin) q = -pivmin;
-  if (q < 0) ++cnt;
+__device__ __forceinline__ int exponent_field(double x) {
+  return (__double2hiint(x) >> 20) & 0x7ff;
+}
+
+// Number of eigenvalues of the tridiagonal (d, e2 = e^2) below x, from the
+// signs of its leading principal minors p_i = (d_i - x) p_{i-1} -
+// e2_{i-1} p_{i-2} (the Sturm sequence; Wilkinson, The Algebraic Eigenvalue
+// Problem, 1965, ch. 5): a sign change from p_{i-1} to p_i is a negative
+// pivot of T - xI = LDL'.  The recurrence needs no division (the FP64 pipe is
+// the bottleneck here).  The pair of latest minors is rescaled by a power of
+// two whenever its larger exponent leaves [2^-400, 2^400], and a minor that
+// comes out exactly zero is replaced, with its predecessor, by the pair
+// (s, -2^-600 s), s = sign of the predecessor: a negative pivot of magnitude
+// 2^-600, as the ratio form replaces a zero pivot by -pivmin.
+__device__ __forceinline__ int sturm_count(const double* d, const double* e2, int n, double x) {
+  double a = 1.0, b = d[0] - x;
+  if (b == 0.0) b = -0x1p-600;
+  int cnt = signbit(b) ? 1 : 0;
   for (int i = 1; i < n; ++i) {
-    q = (d[i] - x) - e2[i - 1] / q;
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0) ++cnt;
+    double c = fma(d[i] - x, b, -e2[i - 1] * a);
+    if ((__double_as_longlong(c) << 1) == 0) {
+      a = copysign(1.0, b);
+      c = -0x1p-600 * a;
+    } else {
+      a = b;
+    }
+    cnt += (signbit(c) != signbit(a)) ? 1 : 0;
+    b = c;
+    const int em = max(exponent_field(a), exponent_field(b));
+    if (em > 1023 + 400 || em < 1023 - 400) {
+      const double s = __hiloint2double((2046 - em) << 20, 0);  // 2^(1023 - em)
+      a *= s;
+      b *= s;
+    }
   }
   return cnt;
 }
 
-// Tridiagonal (d, e) minus theta*I: LU with partial pivoting, then solve in place on y.
-__device__ void tri_solve_shifted(const double* d, const double* e, int n, double theta, double* U0,
-                                  double* U1, double* U2, double* L, double* P, double* y,
-                                  double tiny) {
+// LU with partial pivoting of the tridiagonal (d, e) minus theta*I (Peters &
+// Wilkinson 1971).  Factors are stored with stride ld (one column per
+// eigenvalue): the reciprocal pivots U0i, the two superdiagonals U1, U2 of U,
+// the multipliers L and the row-swap flags P.  Pivots below `tiny` in
+// magnitude are replaced by +-tiny.
+__device__ void tri_factor(const double* d, const double* e, int n, double theta, double* U0i,
+                           double* U1, double* U2, double* L, double* P, int ld, double tiny) {
   double x0 = d[0] - theta, x1 = (n > 1) ? e[0] : 0.0, x2 = 0.0;
   for (int k = 0; k < n - 1; ++k) {
     const double y0 = e[k], y1 = d[k + 1] - theta, y2 = (k + 2 < n) ? e[k + 1] : 0.0;
-    double p0, p1, p2, o0, o1, o2;
-    if (fabs(x0) >= fabs(y0)) {
-      p0 = x0; p1 = x1; p2 = x2; o0 = y0; o1 = y1; o2 = y2; P[k] = 0.0;
-    } else {
-      p0 = y0; p1 = y1; p2 = y2; o0 = x0; o1 = x1; o2 = x2; P[k] = 1.0;
-    }
+    const bool sw = fabs(x0) < fabs(y0);
+    double p0 = sw ? y0 : x0;
+    const double p1 = sw ? y1 : x1, p2 = sw ? y2 : x2;
+    const double o0 = sw ? x0 : y0, o1 = sw ? x1 : y1, o2 = sw ? x2 : y2;
     if (fabs(p0) < tiny) p0 = (p0 < 0 ? -tiny : tiny);
-    const double l = o0 / p0;
-    L[k] = l;
-    U0[k] = p0; U1[k] = p1; U2[k] = p2;
+    const double r = 1.0 / p0;
+    const double l = o0 * r;
+    const int64_t o = (int64_t)k * ld;
+    P[o] = sw ? 1.0 : 0.0;
+    L[o] = l;
+    U0i[o] = r;
+    U1[o] = p1;
+    U2[o] = p2;
     x0 = o1 - l * p1;
     x1 = o2 - l * p2;
     x2 = 0.0;
   }
   if (fabs(x0) < tiny) x0 = (x0 < 0 ? -tiny : tiny);
-  U0[n - 1] = x0; U1[n - 1] = 0.0; U2[n - 1] = 0.0;
-  // forward: row swaps and eliminations on the right-hand side
+  const int64_t o = (int64_t)(n - 1) * ld;
+  U0i[o] = 1.0 / x0;
+  U1[o] = 0.0;
+  U2[o] = 0.0;
+}
+
+// Solve with the factors of tri_factor in place on y (stride ld).
+__device__ void tri_solve(const double* U0i, const double* U1, const double* U2, const double* L,
+                          const double* P, int n, int ld, double* y) {
+  double yk = y[0];
   for (int k = 0; k < n - 1; ++k) {
-    if (P[k] != 0.0) { const double t = y[k]; y[k] = y[k + 1]; y[k + 1] = t; }
-    y[k + 1] -= L[k] * y[k];
+    const int64_t o = (int64_t)k * ld;
+    double yn = y[o + ld];
+    if (P[o] != 0.0) { const double t = yk; yk = yn; yn = t; }
+    y[o] = yk;
+    yk = yn - L[o] * yk;
   }
-  // backward
-  y[n - 1] /= U0[n - 1];
-  if (n > 1) y[n - 2] = (y[n - 2] - U1[n - 2] * y[n - 1]) / U0[n - 2];
-  for (int k = n - 3; k >= 0; --k) y[k] = (y[k] - U1[k] * y[k + 1] - U2[k] * y[k + 2]) / U0[k];
+  const int64_t ol = (int64_t)(n - 1) * ld;
+  double z1 = yk * U0i[ol], z2 = 0.0;  // z_{k+1}, z_{k+2}
+  y[ol] = z1;
+  for (int k = n - 2; k >= 0; --k) {
+    const int64_t o = (int64_t)k * ld;
+    const double z = (y[o] - U1[o] * z1 - U2[o] * z2) * U0i[o];
+    y[o] = z;
+    z2 = z1;
+    z1 = z;
+  }
 }
 
 __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int lda,
@@ -72,6 +124,7 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
                                                               double* theta_all, double* S_all,
                                                               double* work_all, size_t wstride,
                                                               const int32_t* active) {
+  extern __shared__ double svec[];  // v and w of the current reflector (2 lda)
   __shared__ double sh[32];
   __shared__ double s_tau, s_beta, s_K;
   __shared__ int s_skip;
@@ -79,17 +132,16 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
   if (active && !active[b]) return;
   const int n = nsize[b];
   const int t = threadIdx.x;
+  const int lane_e = t & 31, warp_e = t >> 5, nwarp_e = kEigThreads / 32;
   double* A = Aall + (int64_t)b * lda * lda;
   double* W = work_all + (int64_t)b * wstride;
   double* d = W;
   double* e = W + lda;
   double* tau = W + 2 * lda;
-  double* pv = W + 3 * lda;
-  double* e2 = W + 4 * lda;
-  double* vv = W + 5 * lda;
-  double* th = W + 6 * lda;             // want
-  int* clus = (int*)(W + 6 * lda + want);  // want ints (cluster leader flag)
-  double* vecw = W + 6 * lda + 2 * want;   // want * 6 * lda
+  double* e2 = W + 3 * lda;
+  double* th = W + 4 * lda;                // want
+  int* clus = (int*)(W + 4 * lda + want);  // 2 want ints: leader flags, cluster starts
+  double* vecw = W + 4 * lda + 2 * want;   // 5 want lda: LU factors per eigenvalue
   double* theta = theta_all + (int64_t)b * want;
   double* S = S_all + (int64_t)b * lda * want;
   const int nw = min(want, n);
@@ -121,8 +173,12 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
     }
     __syncthreads();
     if (s_skip) continue;
-    // v: v[k+1] = 1, v[i] = A[i][k] * s_beta (stored back into column k)
+    // v: v[k+1] = 1, v[i] = A[i][k] * s_beta, stored in column k and, for a
+    // contiguous copy read by the back-transformation, in row k (row and
+    // column k are not touched by the later steps)
     const int m0 = k + 1;
+    double* vs = svec;
+    double* ws = svec + lda;
     for (int i = m0 + t; i < n; i += kEigThreads) {
       double vi;
       if (i == m0) vi = 1.0;
@@ -130,27 +186,44 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
         vi = A[(int64_t)i * lda + k] * s_beta;
         A[(int64_t)i * lda + k] = vi;
       }
-      vv[i] = vi;
+      A[(int64_t)k * lda + i] = vi;
+      vs[i] = vi;
     }
     __syncthreads();
-    // p = tau * A22 v  (A22 symmetric; thread i reads column i -> coalesced)
+    // p = tau * A22 v: warp per row (A22 is kept symmetric, so row i is
+    // column i), lanes along the row, two rows in flight per warp
     double pdot = 0.0;
-    for (int i = m0 + t; i < n; i += kEigThreads) {
-      double acc = 0.0;
-      for (int j = m0; j < n; ++j) acc += A[(int64_t)j * lda + i] * vv[j];
-      acc *= s_tau;
-      pv[i] = acc;
-      pdot += acc * vv[i];
+    for (int i = m0 + warp_e; i < n; i += 2 * nwarp_e) {
+      const int i2 = i + nwarp_e;
+      const double* Ai = A + (int64_t)i * lda;
+      const double* Ai2 = A + (int64_t)(i2 < n ? i2 : i) * lda;
+      double a1 = 0.0, a2 = 0.0;
+      for (int j = m0 + lane_e; j < n; j += 32) {
+        const double vj = vs[j];
+        a1 = fma(Ai[j], vj, a1);
+        a2 = fma(Ai2[j], vj, a2);
+      }
+      a1 = warp_sum(a1) * s_tau;
+      a2 = warp_sum(a2) * s_tau;
+      if (lane_e == 0) {
+        ws[i] = a1;
+        pdot += a1 * vs[i];
+        if (i2 < n) {
+          ws[i2] = a2;
+          pdot += a2 * vs[i2];
+        }
+      }
     }
     pdot = block_sum(pdot, sh);
     if (t == 0) s_K = -0.5 * s_tau * pdot;
     __syncthreads();
-    for (int i = m0 + t; i < n; i += kEigThreads) pv[i] += s_K * vv[i];  // w
+    for (int i = m0 + t; i < n; i += kEigThreads) ws[i] += s_K * vs[i];  // w
     __syncthreads();
-    // A22 -= v w' + w v'
-    for (int i = m0 + t; i < n; i += kEigThreads) {
-      const double vi = vv[i], wi = pv[i];
-      for (int j = m0; j < n; ++j) A[(int64_t)j * lda + i] -= vv[j] * wi + pv[j] * vi;
+    // A22 -= v w' + w v': warp per row, lanes along the row
+    for (int i = m0 + warp_e; i < n; i += nwarp_e) {
+      double* Ai = A + (int64_t)i * lda;
+      const double vi = vs[i], wi = ws[i];
+      for (int j = m0 + lane_e; j < n; j += 32) Ai[j] -= vs[j] * wi + ws[j] * vi;
     }
     __syncthreads();
   }
@@ -219,90 +292,142 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
   const double pivmin = DBL_MIN * fmax(1.0, emax2) * 4.0;
   gl -= 4.0 * DBL_EPSILON * tnorm + 2 * pivmin;
   gu += 4.0 * DBL_EPSILON * tnorm + 2 * pivmin;
-  for (int j = t; j < nw; j += kEigThreads) {
-    const int idx = n - 1 - j;  // index from the bottom
-    double lo = gl, hi = gu;
-    for (int itb = 0; itb < 200; ++itb) {
-      const double mid = 0.5 * (lo + hi);
-      if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + pivmin || mid == lo || mid == hi) break;
-      if (sturm_count(d, e2, n, mid, pivmin) <= idx) lo = mid; else hi = mid;
+  // multisection: a group of G lanes per eigenvalue probes G interior points
+  // of its interval and keeps the sub-interval where the count passes the
+  // eigenvalue's index
+  {
+    int G = 1;
+    while (G < 32 && 2 * G * nw <= kEigThreads) G *= 2;
+    const int ngroup = kEigThreads / G, sub = t % G, gl0 = (t & 31) - sub;
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gl0);
+    const double frac = 1.0 / (double)(G + 1);
+    for (int j = t / G; j < nw; j += ngroup) {
+      const int idx = n - 1 - j;  // index from the bottom
+      double lo = gl, hi = gu;
+      for (int itb = 0; itb < 200; ++itb) {
+        const double w = hi - lo;
+        if (w <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+        const double x = lo + (double)(sub + 1) * (w * frac);
+        const bool le = sturm_count(d, e2, n, x) <= idx;
+        const unsigned m = (__ballot_sync(gmask, le) & gmask) >> gl0;
+        // the probe just above the highest one at or below the eigenvalue
+        const int kk = (m == 0u) ? 0 : 32 - __clz(m);
+        const double nlo = (kk == 0) ? lo : lo + (double)kk * (w * frac);
+        const double nhi = (kk == G) ? hi : lo + (double)(kk + 1) * (w * frac);
+        if (nlo == lo && nhi == hi) break;
+        lo = nlo;
+        hi = nhi;
+      }
+      if (sub == 0) th[j] = 0.5 * (lo + hi);
     }
-    th[j] = 0.5 * (lo + hi);
   }
   __syncthreads();
 
-  // ---- 3. inverse iteration; clusters of close eigenvalues share one thread
+  // ---- 3. inverse iteration for all wanted eigenvalues at once (thread q
+  // owns eigenvalue q); the vectors live in S (row-major, stride want) and
+  // after each sweep the members of every cluster of close eigenvalues are
+  // orthonormalised by modified Gram-Schmidt, one warp per cluster
+  const int lane = t & 31, warp = t >> 5;
   const double ctol = 1e-7 * fmax(tnorm, DBL_MIN);
+  const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
+  int* lead = clus + want;  // first member of every cluster
   for (int j = t; j < nw; j += kEigThreads) clus[j] = (j == 0) || (th[j - 1] - th[j] > ctol);
   __syncthreads();
-  const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
-  for (int j = t; j < nw; j += kEigThreads) {
-    if (!clus[j]) continue;
-    int jend = j + 1;
-    while (jend < nw && !clus[jend]) ++jend;
-    for (int q = j; q < jend; ++q) {
-      double* U0 = vecw + (int64_t)q * 6 * lda;
-      double* U1 = U0 + lda;
-      double* U2 = U1 + lda;
-      double* Lm = U2 + lda;
-      double* Pv = Lm + lda;
-      double* y = Pv + lda;
-      // shift: separate members of an exact cluster slightly (as LAPACK dstein)
-      double sh_theta = th[q];
-      if (q > j) sh_theta = th[j] - (double)(q - j) * 10.0 * DBL_EPSILON * fmax(fabs(th[j]), tnorm);
-      // deterministic start vector
-      for (int i = 0; i < n; ++i) {
-        unsigned h = (unsigned)(i * 2654435761u) ^ (unsigned)(q * 40503u + 0x9e3779b9u);
-        h ^= h >> 15; h *= 2246822519u; h ^= h >> 13;
-        y[i] = ((double)(h & 0xffffff) / 16777216.0) - 0.5;
-      }
-      for (int itr = 0; itr < 4; ++itr) {
-        tri_solve_shifted(d, e, n, sh_theta, U0, U1, U2, Lm, Pv, y, tiny);
-        // MGS against previous members of the cluster
-        for (int r = j; r < q; ++r) {
-          const double* yr = vecw + (int64_t)r * 6 * lda + 5 * lda;
-          double dp = 0.0;
-          for (int i = 0; i < n; ++i) dp += yr[i] * y[i];
-          for (int i = 0; i < n; ++i) y[i] -= dp * yr[i];
-        }
-        double nrm = 0.0;
-        for (int i = 0; i < n; ++i) nrm += y[i] * y[i];
-        nrm = sqrt(nrm);
-        const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
-        for (int i = 0; i < n; ++i) y[i] *= inv;
-      }
+  if (t == 0) {
+    int c = 0;
+    for (int j = 0; j < nw; ++j)
+      if (clus[j]) lead[c++] = j;
+    s_skip = c;  // number of clusters
+  }
+  double* Y = S;
+  double* U0i = vecw;
+  double* U1 = U0i + (int64_t)lda * want;
+  double* U2 = U1 + (int64_t)lda * want;
+  double* Lm = U2 + (int64_t)lda * want;
+  double* Pv = Lm + (int64_t)lda * want;
+  for (int q = t; q < nw; q += kEigThreads) {
+    int j = q;
+    while (j > 0 && !clus[j]) --j;
+    // members of a cluster get shifts a few ulps apart (as LAPACK dstein)
+    const double shift = th[q] - (double)(q - j) * 10.0 * DBL_EPSILON * fmax(fabs(th[j]), tnorm);
+    tri_factor(d, e, n, shift, U0i + q, U1 + q, U2 + q, Lm + q, Pv + q, want, tiny);
+    for (int i = 0; i < n; ++i) {  // deterministic start vector
+      unsigned h = (unsigned)(i * 2654435761u) ^ (unsigned)(q * 40503u + 0x9e3779b9u);
+      h ^= h >> 15; h *= 2246822519u; h ^= h >> 13;
+      Y[(int64_t)i * want + q] = ((double)(h & 0xffffff) / 16777216.0) - 0.5;
     }
   }
   __syncthreads();
-
-  // ---- 4. back-transformation z = H_0 ... H_{n-3} y  (warp per vector)
-  const int lane = t & 31, warp = t >> 5;
-  for (int q = warp; q < nw; q += kEigThreads / 32) {
-    double* y = vecw + (int64_t)q * 6 * lda + 5 * lda;
-    for (int k = n - 3; k >= 0; --k) {
-      const double tk = tau[k];
-      if (tk == 0.0) continue;
-      double dp = 0.0;
-      for (int i = k + 1 + lane; i < n; i += 32) dp += (i == k + 1 ? 1.0 : A[(int64_t)i * lda + k]) * y[i];
-      dp = warp_sum(dp);
-      for (int i = k + 1 + lane; i < n; i += 32) y[i] -= tk * dp * (i == k + 1 ? 1.0 : A[(int64_t)i * lda + k]);
-      __syncwarp();
+  const int ncl = s_skip;
+  for (int itr = 0; itr < 4; ++itr) {
+    for (int q = t; q < nw; q += kEigThreads) tri_solve(U0i + q, U1 + q, U2 + q, Lm + q, Pv + q, n, want, Y + q);
+    __syncthreads();
+    for (int c = warp; c < ncl; c += kEigThreads / 32) {
+      const int j0 = lead[c], j1 = (c + 1 < ncl) ? lead[c + 1] : nw;
+      for (int m = j0; m < j1; ++m) {
+        for (int r = j0; r < m; ++r) {
+          double dp = 0.0;
+          for (int i = lane; i < n; i += 32) dp += Y[(int64_t)i * want + r] * Y[(int64_t)i * want + m];
+          dp = warp_sum(dp);
+          for (int i = lane; i < n; i += 32) Y[(int64_t)i * want + m] -= dp * Y[(int64_t)i * want + r];
+        }
+        double nrm = 0.0;
+        for (int i = lane; i < n; i += 32) nrm += Y[(int64_t)i * want + m] * Y[(int64_t)i * want + m];
+        nrm = warp_sum(nrm);
+        const double inv = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+        for (int i = lane; i < n; i += 32) Y[(int64_t)i * want + m] *= inv;
+      }
     }
-    for (int i = lane; i < lda; i += 32) S[(int64_t)i * want + q] = (i < n) ? y[i] : 0.0;
-    if (lane == 0) theta[q] = th[q];
+    __syncthreads();
   }
-  // columns beyond n (if want > n) are zero
-  for (int q = nw + warp; q < want; q += kEigThreads / 32) {
-    for (int i = lane; i < lda; i += 32) S[(int64_t)i * want + q] = 0.0;
-    if (lane == 0) theta[q] = 0.0;
+
+  // ---- 4. back-transformation Y <- H_0 ... H_{n-3} Y, one reflector at a
+  // time for all vectors (the reflector is read from its copy in row k):
+  // column dots by (row part, vector) threads, then the rank-1 update
+  constexpr int kBtCols = 64, kBtRows = kEigThreads / kBtCols;
+  const int tx = t % kBtCols, ty = t / kBtCols;
+  double* part = svec;                      // kBtRows x want partial dots
+  double* dps = svec + (int64_t)kBtRows * want;  // want scaled dots
+  for (int k = n - 3; k >= 0; --k) {
+    const double tk = tau[k];
+    if (tk == 0.0) continue;  // uniform: tau is in global memory, read by all
+    const double* vk = A + (int64_t)k * lda;  // vk[k+1] = 1
+    for (int q = tx; q < nw; q += kBtCols) {
+      double acc = 0.0;
+      for (int i = k + 1 + ty; i < n; i += kBtRows) acc = fma(vk[i], Y[(int64_t)i * want + q], acc);
+      part[ty * want + q] = acc;
+    }
+    __syncthreads();
+    for (int q = t; q < nw; q += kEigThreads) {
+      double s = 0.0;
+      for (int r = 0; r < kBtRows; ++r) s += part[r * want + q];
+      dps[q] = tk * s;
+    }
+    __syncthreads();
+    for (int i = k + 1 + ty; i < n; i += kBtRows) {
+      const double vi = vk[i];
+      for (int q = tx; q < nw; q += kBtCols) Y[(int64_t)i * want + q] -= dps[q] * vi;
+    }
+    __syncthreads();
   }
+  // rows beyond n and columns beyond nw (if want > n) are zero
+  for (int i = ty; i < lda; i += kBtRows)
+    for (int q = tx; q < want; q += kBtCols)
+      if (i >= n || q >= nw) Y[(int64_t)i * want + q] = 0.0;
+  for (int q = t; q < want; q += kEigThreads) theta[q] = (q < nw) ? th[q] : 0.0;
 }
 
 int sym_eig_top(int nmat, double* A, int lda, const int32_t* nsize, int want, double* theta,
                 double* S, double* work, const int32_t* active, cudaStream_t stream) {
   if (nmat <= 0) return LAPY_OK;
-  sym_eig_kernel<<<nmat, kEigThreads, 0, stream>>>(A, lda, nsize, want, theta, S, work,
-                                                  sym_eig_work_doubles(lda, want), active);
+  // v and w of a reflector (2 lda), partial dots of the back-transformation
+  // (5 want)
+  const size_t smem = sizeof(double) * std::max<size_t>(2 * (size_t)lda, 5 * (size_t)want);
+  if (smem > 48 * 1024) {
+    LAPY_CUDA_TRY(cudaFuncSetAttribute(sym_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  sym_eig_kernel<<<nmat, kEigThreads, smem, stream>>>(A, lda, nsize, want, theta, S, work,
+                                                     sym_eig_work_doubles(lda, want), active);
   return lapy_check_launch("sym_eig_kernel");
 }
 
