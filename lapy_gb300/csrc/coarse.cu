@@ -8,6 +8,7 @@
 // segment (one thread per coarse row, fixed summation order) and its dense
 // inverse (one CTA per segment: FP64 Cholesky, triangular inverse, B'B),
 // stored in FP32 for the per-iteration coarse product of the PCG.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -45,12 +46,13 @@ static int64_t max_coarse_entries(const int32_t* seg_row, int nseg) {
   return t;
 }
 
-size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg) {
+size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg, int nvc) {
   const int64_t na = two_level_max_aggs(seg_row, nseg);
   const int64_t ne = max_coarse_entries(seg_row, nseg);
   return a256(4 * (size_t)n) * 2 + a256(4 * (size_t)(na + 1)) + a256(4 * (size_t)na) +
          a256(4 * (size_t)(nseg + 1)) + a256(8 * (size_t)(nseg + 1)) + a256(4 * (size_t)ne) +
-         a256(8 * (size_t)ne) + a256(4 * (size_t)nseg) + 1024;
+         a256(8 * (size_t)ne) + a256(4 * (size_t)nseg) + a256(4 * (size_t)(std::max(nvc, 1) + 1)) +
+         a256(4 * (size_t)(nseg + 1)) + a256(4 * (size_t)std::max(nseg, 1)) + 1024;
 }
 
 // ---- host aggregation -------------------------------------------------------
@@ -257,9 +259,10 @@ __global__ void __launch_bounds__(kInvThreads) coarse_inverse_kernel(const int32
 }
 
 int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64,
-                    const int32_t* seg_row, int nseg, void* mem, size_t bytes, PcgPrecondDesc<float>* pc,
-                    cudaStream_t stream) {
-  if (bytes < two_level_bytes(n, seg_row, nseg)) return LAPY_ERR_WORKSPACE;
+                    const int32_t* seg_row, int nseg, int nvc, void* mem, size_t bytes,
+                    PcgPrecondDesc<float>* pc, cudaStream_t stream) {
+  nvc = std::max(nvc, 1);
+  if (bytes < two_level_bytes(n, seg_row, nseg, nvc)) return LAPY_ERR_WORKSPACE;
   // pattern to the host
   std::vector<int32_t> hptr(n + 1);
   LAPY_CUDA_TRY(cudaMemcpyAsync(hptr.data(), indptr, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, stream));
@@ -303,6 +306,28 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
       if (agg[v] >= 0) agg_row[fill[agg[v]]++] = (int32_t)v;
   }
 
+  // the coarse work (a restriction over the aggregate's rows and one row of
+  // the segment's dense inverse per aggregate) split over the virtual CTAs in
+  // contiguous ranges of equal aggregate counts (the time of a coarse row is
+  // mostly the latency of its dependent loads and warp reductions, so counts
+  // balance better than bytes), and the reduction slots of each segment's
+  // coarse partial sums
+  std::vector<int32_t> vc_agg(nvc + 1, 0), seg_aslot(nseg + 1, 0), seg_avc0(std::max(nseg, 1), 0);
+  {
+    for (int v = 0; v <= nvc; ++v) vc_agg[v] = (int32_t)((int64_t)nagg * v / nvc);
+    auto vc_of = [&](int32_t g) {
+      return (int)(std::upper_bound(vc_agg.begin(), vc_agg.end(), g) - vc_agg.begin()) - 1;
+    };
+    for (int s = 0; s < nseg; ++s) {
+      int ns = 0;
+      if (nc[s] > 0) {
+        seg_avc0[s] = vc_of(seg_agg[s]);
+        ns = vc_of(seg_agg[s + 1] - 1) - seg_avc0[s] + 1;
+      }
+      seg_aslot[s + 1] = seg_aslot[s] + ns;
+    }
+  }
+
   // device layout
   char* w = (char*)(((uintptr_t)mem + 255) & ~uintptr_t(255));
   const int64_t na_max = two_level_max_aggs(seg_row, nseg);
@@ -319,6 +344,9 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   int64_t* d_off = (int64_t*)w; w += a256(8 * (size_t)(nseg + 1));
   float* d_kinv = (float*)w; w += a256(4 * (size_t)ne_max);
   double* d_kc = (double*)w; w += a256(8 * (size_t)ne_max);
+  int32_t* d_vca = (int32_t*)w; w += a256(4 * (size_t)(nvc + 1));
+  int32_t* d_asl = (int32_t*)w; w += a256(4 * (size_t)(nseg + 1));
+  int32_t* d_av0 = (int32_t*)w; w += a256(4 * (size_t)std::max(nseg, 1));
   int* d_fail = (int*)w;
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_agg, agg.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
   if (!agg_row.empty())
@@ -328,6 +356,9 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
     LAPY_CUDA_TRY(cudaMemcpyAsync(d_sid, agg_sid.data(), 4 * (size_t)nagg, cudaMemcpyHostToDevice, stream));
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_seg, seg_agg.data(), 4 * seg_agg.size(), cudaMemcpyHostToDevice, stream));
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_off, off.data(), 8 * off.size(), cudaMemcpyHostToDevice, stream));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_vca, vc_agg.data(), 4 * vc_agg.size(), cudaMemcpyHostToDevice, stream));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_asl, seg_aslot.data(), 4 * seg_aslot.size(), cudaMemcpyHostToDevice, stream));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_av0, seg_avc0.data(), 4 * seg_avc0.size(), cudaMemcpyHostToDevice, stream));
   if (off[nseg] > 0) LAPY_CUDA_TRY(cudaMemsetAsync(d_kc, 0, 8 * (size_t)off[nseg], stream));
   LAPY_CUDA_TRY(cudaMemsetAsync(d_fail, 0, 4 * (size_t)nseg, stream));
   if (nagg > 0) {
@@ -348,6 +379,11 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   pc->seg_agg = d_seg;
   pc->kinv_off = d_off;
   pc->kinv = d_kinv;
+  pc->nvc = nvc;
+  pc->naslot = seg_aslot[nseg];
+  pc->vc_agg = d_vca;
+  pc->seg_aslot = d_asl;
+  pc->seg_avc0 = d_av0;
   return LAPY_OK;
 }
 

@@ -19,14 +19,15 @@ constexpr int kCoarseMaxDim = 2048;
 // Upper bounds used to size the caller's workspace: aggregates over all
 // segments, and bytes of device memory for the two-level data.
 int64_t two_level_max_aggs(const int32_t* seg_row, int nseg);
-size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg);
+size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg, int nvc);
 
 // Build the coarse space of K (CSR on the device, FP64 values) for the
 // segments seg_row (host): aggregation on the host, Galerkin matrix W'KW and
-// its dense inverse (FP64 Cholesky, stored FP32) on the device.  Fills the
-// two-level fields of `pc` (which keeps its Jacobi diagonal).
+// its dense inverse (FP64 Cholesky, stored FP32) on the device, and the
+// split of the coarse work over the nvc virtual CTAs of the PCG's warp plan.
+// Fills the two-level fields of `pc` (which keeps its Jacobi diagonal).
 int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64,
-                    const int32_t* seg_row, int nseg, void* mem, size_t bytes, PcgPrecondDesc<float>* pc,
-                    cudaStream_t stream);
+                    const int32_t* seg_row, int nseg, int nvc, void* mem, size_t bytes,
+                    PcgPrecondDesc<float>* pc, cudaStream_t stream);
 
 }  // namespace lapy

@@ -86,52 +86,76 @@ __device__ __forceinline__ T block_sum(T v, T* sh) {
 //
 // The kernels that use it are launched with cudaLaunchCooperativeKernel, so
 // every CTA is resident and the barrier completes.  The spin is still bounded:
-// after LAPY_BARRIER_SPIN_LIMIT polls the waiting CTA records LAPY_ERR_TIMEOUT
-// in *err and leaves; every CTA checks *err after each barrier and returns.
+// after LAPY_BARRIER_SPIN_LIMIT polls the waiting CTA marks the barrier word
+// as failed, records LAPY_ERR_TIMEOUT in *err and leaves; every CTA that
+// arrives or polls afterwards sees the mark and returns.
 // ---------------------------------------------------------------------------
 #ifndef LAPY_BARRIER_SPIN_LIMIT
 #define LAPY_BARRIER_SPIN_LIMIT (1u << 26)
 #endif
 
+// One 64-bit word, cleared before the launch and alone on its cache line:
+// bits 0-31 count arrivals (barrier g completes when they reach (g+1) CTAs),
+// bits 32-62 sum the flags the CTAs pass in (so a barrier also tells every
+// CTA how many CTAs raised a flag), bit 63 marks a failure.  A CTA whose wait
+// times out sets bit 63, which every later poll and arrival sees, and records
+// LAPY_ERR_TIMEOUT in *err for the host.
 struct GridBarrier {
-  unsigned int* count;  // arrivals in the current generation
-  unsigned int* gen;    // generation counter
-  int* err;             // sticky error flag (0 = ok)
+  unsigned long long* word;
+  int* err;  // sticky error flag (0 = ok)
 };
+constexpr unsigned long long kBarrierFail = 1ull << 63;
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ int ld_volatile_i32(const int* p) {
   return *((volatile const int*)p);
 }
 
-// Returns true when the grid may continue, false when an error was recorded.
-__device__ __forceinline__ bool grid_sync(const GridBarrier& b) {
+// Barrier over all CTAs of the grid.  *s_flag (shared) is this CTA's flag
+// (0 or 1), read and cleared here; *s_seen (shared) receives the flag sum
+// (bits 32-62 of the word) when the barrier completed.  Returns false when a
+// failure was recorded.  Pass nullptr for both to ignore flags.
+__device__ __forceinline__ bool grid_sync(const GridBarrier& b, int* s_flag = nullptr,
+                                          unsigned* s_seen = nullptr) {
+  __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
-    const unsigned my_gen = ld_acquire_u32(b.gen);
-    __threadfence();
-    const unsigned arrived = atomicAdd(b.count, 1u);
-    if (arrived == nblocks - 1) {
-      atomicExch(b.count, 0u);
-      __threadfence();
-      atomicAdd(b.gen, 1u);
-    } else {
-      unsigned spins = 0;
-      while (ld_acquire_u32(b.gen) == my_gen) {
-        if (++spins > LAPY_BARRIER_SPIN_LIMIT) {
-          atomicCAS(b.err, 0, LAPY_ERR_TIMEOUT);
-          break;
-        }
-        if (spins > 64) __nanosleep(64);
-      }
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+    unsigned long long add = 1ull;
+    if (s_flag) {
+      if (*s_flag) add += 1ull << 32;
+      *s_flag = 0;
     }
     __threadfence();
+    const unsigned long long old = atomicAdd(b.word, add);
+    unsigned long long v = old + add;
+    bool ok = (old & kBarrierFail) == 0ull;
+    const unsigned target = ((unsigned)old / nb + 1u) * nb;
+    unsigned spins = 0;
+    while (ok && (int)((unsigned)v - target) < 0) {
+      if (++spins > LAPY_BARRIER_SPIN_LIMIT) {
+        atomicOr(b.word, kBarrierFail);
+        atomicCAS(b.err, 0, LAPY_ERR_TIMEOUT);
+        ok = false;
+        break;
+      }
+      if (spins > 64) __nanosleep(64);
+      v = ld_acquire_u64(b.word);
+      if (v & kBarrierFail) ok = false;
+    }
+    __threadfence();
+    if (s_seen) *s_seen = (unsigned)((v >> 32) & 0x7fffffffull);
+    s_ok = ok ? 1 : 0;
   }
   __syncthreads();
-  return ld_volatile_i32(b.err) == 0;
+  return s_ok != 0;
 }

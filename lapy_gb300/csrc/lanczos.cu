@@ -717,7 +717,7 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.MW = (double*)take(8 * n * p);
   e.ir_bytes = ir_workspace_bytes(n, p, P.ct, 1, P.precond, P.nagg_max);
   e.ir_ws = take(e.ir_bytes);
-  e.tl_bytes = P.precond == kPrecTwoLevel ? two_level_bytes(n, P.ct.h_seg_row.data(), ns) : 0;
+  e.tl_bytes = P.precond == kPrecTwoLevel ? two_level_bytes(n, P.ct.h_seg_row.data(), ns, P.ct.nvc) : 0;
   e.tl_mem = take(e.tl_bytes);
   e.sell_bytes = sell_bytes_bound(nnz, P.ct, sizeof(float));
   e.sell_mem = take(e.sell_bytes);
@@ -960,7 +960,8 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     }
   }
   if (P.precond == kPrecTwoLevel)
-    LAPY_TRY(build_two_level(n, indptr, indices, e.k64, P.ct.h_seg_row.data(), ns, e.tl_mem, e.tl_bytes, &K.pc32, st));
+    LAPY_TRY(build_two_level(n, indptr, indices, e.k64, P.ct.h_seg_row.data(), ns, P.ct.nvc, e.tl_mem,
+                                    e.tl_bytes, &K.pc32, st));
 
   LAPY_CUDA_TRY(cudaMemsetAsync(e.rcnt, 0, 16, st));
   std::vector<int32_t> hact(ns, 1), hnsize(ns, 0);

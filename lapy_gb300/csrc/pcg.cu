@@ -63,16 +63,23 @@ int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable*
   ct->h_unit_row.push_back(seg_row[nseg]);
   ct->nunit = (int)unit_seg.size();
 
-  // virtual warps: contiguous unit ranges with about total/nvw rows each
-  const int nvw = std::max(1, std::min(ct->nunit, kPlanCtasPerSm * kWarps * lapy_num_sms()));
-  ct->nvw = nvw;
-  std::vector<int32_t> ub(nvw + 1);
-  for (int w = 0; w <= nvw; ++w) {
-    const int64_t target = seg_row[0] + total * w / nvw;
-    ub[w] = (int32_t)(std::lower_bound(ct->h_unit_row.begin(), ct->h_unit_row.begin() + ct->nunit,
-                                       (int32_t)target) - ct->h_unit_row.begin());
+  // virtual warps: contiguous unit ranges with about total/nvw rows each;
+  // ranges that received no unit are dropped, so every virtual warp (and
+  // every virtual CTA below) holds at least one piece
+  const int nvw0 = std::max(1, std::min(ct->nunit, kPlanCtasPerSm * kWarps * lapy_num_sms()));
+  std::vector<int32_t> ub;
+  ub.reserve(nvw0 + 1);
+  ub.push_back(0);
+  for (int w = 1; w <= nvw0; ++w) {
+    const int64_t target = seg_row[0] + total * w / nvw0;
+    int32_t b = (int32_t)(std::lower_bound(ct->h_unit_row.begin(), ct->h_unit_row.begin() + ct->nunit,
+                                           (int32_t)target) - ct->h_unit_row.begin());
+    if (w == nvw0) b = ct->nunit;
+    if (b > ub.back()) ub.push_back(b);
   }
-  ub[nvw] = ct->nunit;
+  if (ub.size() == 1) ub.push_back(ct->nunit);  // no units at all: one empty virtual warp
+  const int nvw = (int)ub.size() - 1;
+  ct->nvw = nvw;
   ct->h_piece_unit.clear();
   ct->h_piece_seg.clear();
   ct->h_vw_piece.assign(nvw + 1, 0);
@@ -92,13 +99,35 @@ int plan_chunks(const int32_t* seg_row, int nseg, int target_chunks, ChunkTable*
   for (int p = ct->npiece - 1; p >= 0; --p) ct->h_seg_piece[ct->h_piece_seg[p]] = p;
   for (int s = nseg - 1; s >= 0; --s)  // segments without rows: empty piece range
     if (ct->h_seg_piece[s] > ct->h_seg_piece[s + 1]) ct->h_seg_piece[s] = ct->h_seg_piece[s + 1];
+
+  // virtual CTAs and the reduction slots of every segment
+  const int nvc = (nvw + kWarps - 1) / kWarps;
+  ct->nvc = nvc;
+  ct->h_vc_piece.resize(nvc + 1);
+  for (int v = 0; v <= nvc; ++v) ct->h_vc_piece[v] = ct->h_vw_piece[std::min(v * kWarps, nvw)];
+  std::vector<int32_t> piece_vc(ct->npiece);
+  for (int w = 0; w < nvw; ++w)
+    for (int32_t q = ct->h_vw_piece[w]; q < ct->h_vw_piece[w + 1]; ++q) piece_vc[q] = w / kWarps;
+  ct->h_seg_slot.assign(nseg + 1, 0);
+  ct->h_seg_vc0.assign(nseg, 0);
+  for (int s = 0; s < nseg; ++s) {
+    const int32_t q0 = ct->h_seg_piece[s], q1 = ct->h_seg_piece[s + 1];
+    int ns = 0;
+    if (q0 < q1) {
+      ct->h_seg_vc0[s] = piece_vc[q0];
+      ns = piece_vc[q1 - 1] - piece_vc[q0] + 1;
+    }
+    ct->h_seg_slot[s + 1] = ct->h_seg_slot[s] + ns;
+  }
+  ct->nslot = ct->h_seg_slot[nseg];
   return ct->nchunk;
 }
 
 size_t chunk_table_bytes(const ChunkTable& ct) {
   return a256(4 * (size_t)(ct.nchunk + 1)) + a256(4 * (size_t)ct.nchunk) + a256(4 * (size_t)(ct.nseg + 1)) * 3 +
          a256(4 * (size_t)(ct.nunit + 1)) + a256(4 * (size_t)(ct.npiece + 1)) + a256(4 * (size_t)ct.npiece) +
-         a256(4 * (size_t)(ct.nvw + 1));
+         a256(4 * (size_t)(ct.nvw + 1)) + a256(4 * (size_t)(ct.nvc + 1)) + a256(4 * (size_t)(ct.nseg + 1)) +
+         a256(4 * (size_t)std::max(ct.nseg, 1));
 }
 
 int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream) {
@@ -118,6 +147,9 @@ int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream) {
   LAPY_TRY(put(&ct->piece_seg, ct->h_piece_seg));
   LAPY_TRY(put(&ct->vw_piece, ct->h_vw_piece));
   LAPY_TRY(put(&ct->seg_piece, ct->h_seg_piece));
+  LAPY_TRY(put(&ct->vc_piece, ct->h_vc_piece));
+  LAPY_TRY(put(&ct->seg_slot, ct->h_seg_slot));
+  LAPY_TRY(put(&ct->seg_vc0, ct->h_seg_vc0));
   // pageable sources: the copies must complete before the host vectors change
   LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
   return LAPY_OK;
@@ -142,9 +174,14 @@ struct PcgArgs {
   const int32_t* piece_seg;
   const int32_t* vw_piece;
   const int32_t* seg_piece;
+  const int32_t* vc_piece;  // virtual CTAs (8 virtual warps) and reduction slots
+  const int32_t* seg_slot;
+  const int32_t* seg_vc0;
   int nvw;
   int npiece;
   int nseg;
+  int nvc;
+  int nslot;
   const V* B;
   V* X;
   V* R;
@@ -153,6 +190,8 @@ struct PcgArgs {
   V* Z;
   V* T;
   S* part;            // [3][npiece][NP]  pq, rz, rr
+  S* slot;            // [3][nslot][NP]   the same folded per virtual CTA
+  S* aslot;           // [naslot][NP]     csl folded per virtual CTA (two-level)
   S* rc;              // [nagg][NP] restricted residual W'r   (two-level)
   S* yc;              // [nagg][NP] coarse solution (W'KW)^-1 W'r
   S* csl;             // [nagg][NP] rc .* yc (coarse part of r'z)
@@ -160,7 +199,6 @@ struct PcgArgs {
   S* bb;              // [nseg][NP]
   int32_t* state;     // [2][nseg][NP]
   int32_t* state_out; // [nseg][NP]
-  unsigned* active;   // [2]
   int* iters;         // [1]
   unsigned long long* work;  // [2] rows and nonzeros processed by the SpMM phase
   S rtol2;
@@ -172,6 +210,7 @@ struct PcgArgs {
   double* X64;         // n x NP
   const double* K64;   // FP64 values on indptr / indices
   double* part64;      // [npiece][NP]  partial ||b - K x||^2
+  double* slot64;      // [nslot][NP]   the same folded per virtual CTA
   S* rref;             // [nseg][NP]    squared residual at the last update
   int32_t* ru_col;     // [2][nseg][NP] update requests (by parity)
   unsigned* ru_flag;   // [2]           any request (by parity)
@@ -228,16 +267,59 @@ __device__ __forceinline__ void store_row(V* __restrict__ base, int64_t row, con
 // Sum of a segment's piece slots for every column; afterwards each lane holds
 // all NP totals in tot[] (fixed summation order).  FP32 throughout: the
 // iteration's vectors are FP32, and FP64 arithmetic is scarce on this part.
+// The slots [p0, p1) form one contiguous array of (p1 - p0) * NP values; when
+// NP spans two or more 16-byte vectors, lanes stream it as vectors (a lane
+// always lands on the same VEC columns), two vectors in flight per lane, so
+// a segment of a few hundred pieces costs a few memory round trips; narrower
+// rows keep one value per lane with four loads in flight (fewer registers).
 template <int NP, typename S>
 __device__ __forceinline__ void seg_totals(const S* __restrict__ part, int p0, int p1, S (&tot)[NP]) {
   const int lane = threadIdx.x & 31;
-  constexpr int SPAN = (NP <= 32) ? 32 / NP : 1;
-  S acc = S(0);
-  for (int p = p0 + lane / NP; p < p1; p += SPAN) acc += part[(int64_t)p * NP + (lane % NP)];
+  constexpr int VEC = 16 / (int)sizeof(S);
+  if constexpr (NP % VEC == 0 && NP >= 2 * VEC && NP <= 32 * VEC) {
+    using Vec = typename std::conditional<sizeof(S) == 4, float4, double2>::type;
+    const Vec* base = reinterpret_cast<const Vec*>(part + (int64_t)p0 * NP);
+    const int nv = (p1 - p0) * (NP / VEC);
+    S acc[VEC];
 #pragma unroll
-  for (int o = 16; o >= NP; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    for (int j = 0; j < VEC; ++j) acc[j] = S(0);
+    auto add = [&](const Vec& v) {
+      if constexpr (sizeof(S) == 4) {
+        acc[0] += v.x; acc[1] += v.y; acc[2 % VEC] += v.z; acc[3 % VEC] += v.w;
+      } else {
+        acc[0] += v.x; acc[1 % VEC] += v.y;
+      }
+    };
+    int i = lane;
+    for (; i + 32 < nv; i += 64) {
+      const Vec v0 = base[i], v1 = base[i + 32];
+      add(v0); add(v1);
+    }
+    if (i < nv) add(base[i]);
+    // lanes l and l' hold the same columns when l = l' mod NP / VEC
 #pragma unroll
-  for (int q = 0; q < NP; ++q) tot[q] = __shfl_sync(0xffffffffu, acc, q);
+    for (int o = 16; o >= NP / VEC && o > 0; o >>= 1) {
+#pragma unroll
+      for (int j = 0; j < VEC; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+    }
+#pragma unroll
+    for (int q = 0; q < NP; ++q) tot[q] = __shfl_sync(0xffffffffu, acc[q % VEC], q / VEC);
+  } else {
+    constexpr int SPAN = (NP <= 32) ? 32 / NP : 1;
+    S acc = S(0);
+    int p = p0 + lane / NP;
+    for (; p + 3 * SPAN < p1; p += 4 * SPAN) {
+      const S a0 = part[(int64_t)p * NP + (lane % NP)], a1 = part[(int64_t)(p + SPAN) * NP + (lane % NP)];
+      const S a2 = part[(int64_t)(p + 2 * SPAN) * NP + (lane % NP)];
+      const S a3 = part[(int64_t)(p + 3 * SPAN) * NP + (lane % NP)];
+      acc += (a0 + a1) + (a2 + a3);
+    }
+    for (; p < p1; p += SPAN) acc += part[(int64_t)p * NP + (lane % NP)];
+#pragma unroll
+    for (int o = 16; o >= NP; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+#pragma unroll
+    for (int q = 0; q < NP; ++q) tot[q] = __shfl_sync(0xffffffffu, acc, q);
+  }
 }
 
 // Warp-reduce per-lane column partials and store them to dst[0..NP).
@@ -332,14 +414,75 @@ __device__ __forceinline__ void sell_unit_spmm(const SellMatrix<V>& M, const V* 
   }
 }
 
+// Reduction slots.  After the warps of a CTA have stored the partial sums of
+// their pieces (and after a __syncthreads), the CTA folds them into one slot
+// per (segment, virtual CTA), one warp per segment, in piece order; consumers
+// then sum a segment's slots, at most one per CTA that holds rows of it,
+// instead of one per piece.
+template <typename V, int NP, typename S>
+__device__ __forceinline__ void fold_pieces(const PcgArgs<V>& a, const S* __restrict__ part,
+                                            S* __restrict__ slots) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int vc = blockIdx.x; vc < a.nvc; vc += gridDim.x) {
+    const int p0 = a.vc_piece[vc], p1 = a.vc_piece[vc + 1];
+    if (p0 >= p1) continue;
+    const int s0 = a.piece_seg[p0], s1 = a.piece_seg[p1 - 1];
+    for (int s = s0 + warp; s <= s1; s += kWarps) {
+      const int pa = max(a.seg_piece[s], p0), pb = min(a.seg_piece[s + 1], p1);
+      if (pa >= pb) continue;
+      S tot[NP];
+      seg_totals<NP>(part, pa, pb, tot);
+      S* dst = slots + (int64_t)(a.seg_slot[s] + vc - a.seg_vc0[s]) * NP;
+#pragma unroll
+      for (int q = 0; q < NP; ++q)
+        if (lane == q) dst[q] = tot[q];
+    }
+  }
+}
+
+// Visit the aggregates (coarse unknowns) this warp handles: those of the
+// CTA's virtual CTAs (contiguous ranges of about equal coarse work), every
+// kWarps-th one starting at the warp's index; s is the aggregate's segment.
+#define FOR_MY_AGGS(a, ...)                                                                 \
+  for (int vc = blockIdx.x; vc < (a).pc.nvc; vc += gridDim.x) {                            \
+    for (int g = (a).pc.vc_agg[vc] + (int)(threadIdx.x >> 5); g < (a).pc.vc_agg[vc + 1];   \
+         g += kWarps) {                                                                    \
+      const int s = (a).pc.agg_sid[g];                                                     \
+      __VA_ARGS__                                                                          \
+    }                                                                                      \
+  }
+
+// Fold the per-aggregate csl values of the CTA's virtual CTAs into one slot
+// per (segment, virtual CTA), one warp per segment (after a __syncthreads).
+template <typename V, int NP, typename S>
+__device__ __forceinline__ void fold_aggs(const PcgArgs<V>& a, const S* __restrict__ csl,
+                                          S* __restrict__ slots) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int vc = blockIdx.x; vc < a.pc.nvc; vc += gridDim.x) {
+    const int g0 = a.pc.vc_agg[vc], g1 = a.pc.vc_agg[vc + 1];
+    if (g0 >= g1) continue;
+    const int s0 = a.pc.agg_sid[g0], s1 = a.pc.agg_sid[g1 - 1];
+    for (int s = s0 + warp; s <= s1; s += kWarps) {
+      const int ga = max(a.pc.seg_agg[s], g0), gb = min(a.pc.seg_agg[s + 1], g1);
+      if (ga >= gb) continue;
+      S tot[NP];
+      seg_totals<NP>(csl, ga, gb, tot);
+      S* dst = slots + (int64_t)(a.pc.seg_aslot[s] + vc - a.pc.seg_avc0[s]) * NP;
+#pragma unroll
+      for (int q = 0; q < NP; ++q)
+        if (lane == q) dst[q] = tot[q];
+    }
+  }
+}
+
 // Two-level preconditioner, restriction: rc = W' R for the aggregates of
-// segments with an active column (all == true: every aggregate).
+// segments with an active column (all == true: every aggregate), one warp
+// per aggregate.
 template <typename V, int NP>
-__device__ __forceinline__ void coarse_restrict(const PcgArgs<V>& a, const int32_t* st, bool all, int gw, int nw) {
+__device__ __forceinline__ void coarse_restrict(const PcgArgs<V>& a, const int32_t* st, bool all) {
   using S = ScalarOf<V>;
   const int lane = threadIdx.x & 31;
-  for (int g = gw; g < a.pc.nagg; g += nw) {
-    const int s = a.pc.agg_sid[g];
+  FOR_MY_AGGS(a, {
     if (!all) {
       bool act = false;
 #pragma unroll
@@ -360,17 +503,16 @@ __device__ __forceinline__ void coarse_restrict(const PcgArgs<V>& a, const int32
       const S v = warp_sum(acc[q]);
       if (lane == q) a.rc[(int64_t)g * NP + q] = v;
     }
-  }
+  })
 }
 
 // Two-level preconditioner, coarse solve: yc = (W'KW)^-1 rc per segment (one
 // warp per coarse row) and csl = rc .* yc.
 template <typename V, int NP>
-__device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t* st, bool all, int gw, int nw) {
+__device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t* st, bool all) {
   using S = ScalarOf<V>;
   const int lane = threadIdx.x & 31;
-  for (int g = gw; g < a.pc.nagg; g += nw) {
-    const int s = a.pc.agg_sid[g];
+  FOR_MY_AGGS(a, {
     if (!all) {
       bool act = false;
 #pragma unroll
@@ -397,7 +539,9 @@ __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t*
         a.csl[(int64_t)g * NP + q] = y * a.rc[(int64_t)g * NP + q];
       }
     }
-  }
+  })
+  __syncthreads();
+  fold_aggs<V, NP>(a, a.csl, a.aslot);
 }
 
 // z = dinv .* r (+ the coarse correction W yc for the two-level preconditioner)
@@ -487,7 +631,17 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
   S* part_pq = a.part;
   S* part_rz = a.part + (int64_t)a.npiece * NP;
   S* part_rr = a.part + 2 * (int64_t)a.npiece * NP;
+  S* slot_pq = a.slot;
+  S* slot_rz = a.slot + (int64_t)a.nslot * NP;
+  S* slot_rr = a.slot + 2 * (int64_t)a.nslot * NP;
   constexpr bool kDiagPC = PC == kPrecJacobi || PC == kPrecTwoLevel;  // z = dinv .* r (+ coarse term)
+  // CTA flag "a column of one of my segments is still active", summed over
+  // the grid by the barriers that close the initialisation and phase C
+  __shared__ int s_act;
+  __shared__ unsigned s_seen;
+  if (threadIdx.x == 0) s_act = 0;
+  // rows and nonzeros this warp streamed through the SpMM phase
+  unsigned long long w_rows = 0, w_nnz = 0;
 
   // ---- phase 0: X = 0, R = B, P = M^-1 R (Jacobi); partial b'b and r'z
   FOR_MY_PIECES(a, {
@@ -524,11 +678,14 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     warp_store_partials<NP>(bb, part_rr + (int64_t)p * NP);
     if (kDiagPC) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
   })
+  __syncthreads();
+  fold_pieces<V, NP>(a, part_rr, slot_rr);
+  if (kDiagPC) fold_pieces<V, NP>(a, part_rz, slot_rz);
   if constexpr (PC == kPrecTwoLevel) {
     if (!grid_sync(a.bar)) return;
-    coarse_restrict<V, NP>(a, nullptr, true, gw, nw);
+    coarse_restrict<V, NP>(a, nullptr, true);
     if (!grid_sync(a.bar)) return;
-    coarse_solve<V, NP>(a, nullptr, true, gw, nw);
+    coarse_solve<V, NP>(a, nullptr, true);
   }
   if constexpr (PC == kPrecFactored) {  // r'z = ||G r||^2; P = G'(G r) below
     if (!grid_sync(a.bar)) return;
@@ -539,6 +696,8 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       factor_first_half<V, NP>(a, u0, u1, acc);
       warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
     })
+    __syncthreads();
+    fold_pieces<V, NP>(a, part_rz, slot_rz);
   }
   if (!grid_sync(a.bar)) return;
   // ---- segment initialisation (the warp holding a segment's first piece publishes)
@@ -565,11 +724,11 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     }
     if (a.seg_piece[s] == p) {
       S bb[NP], rz[NP];
-      seg_totals<NP>(part_rr, a.seg_piece[s], a.seg_piece[s + 1], bb);
-      seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rz);
+      seg_totals<NP>(slot_rr, a.seg_slot[s], a.seg_slot[s + 1], bb);
+      seg_totals<NP>(slot_rz, a.seg_slot[s], a.seg_slot[s + 1], rz);
       if constexpr (PC == kPrecTwoLevel) {
         S c[NP];
-        seg_totals<NP>(a.csl, a.pc.seg_agg[s], a.pc.seg_agg[s + 1], c);
+        seg_totals<NP>(a.aslot, a.pc.seg_aslot[s], a.pc.seg_aslot[s + 1], c);
 #pragma unroll
         for (int q = 0; q < NP; ++q) rz[q] += c[q];
       }
@@ -585,12 +744,13 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
           a.rz[s * NP + q] = rz[q];
           if (RU) a.rref[s * NP + q] = bb[q];
           a.state[s * NP + q] = st;
-          if (st == kActive) atomicAdd(&a.active[0], 1u);
+          if (st == kActive) s_act = 1;
         }
       }
     }
   })
-  if (!grid_sync(a.bar)) return;
+  if (!grid_sync(a.bar, &s_act, &s_seen)) return;
+  unsigned seen_prev = s_seen, nact = s_seen;
 
   int it = 0;
   for (;; ++it) {
@@ -599,7 +759,6 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     int32_t* st_nxt = a.state + (par ^ 1) * (int64_t)a.nseg * NP;
     const S* rz_cur = a.rz + par * (int64_t)a.nseg * NP;
     S* rz_nxt = a.rz + (par ^ 1) * (int64_t)a.nseg * NP;
-    const unsigned nact = *((volatile unsigned*)&a.active[par]);
     if (nact == 0 || it >= a.maxiter) break;
 
     // ---- reliable update of the columns flagged in the previous phase C:
@@ -677,16 +836,16 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
           warp_store_partials<NP>(rr, a.part64 + (int64_t)p * NP);
           warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
         })
+        __syncthreads();
+        fold_pieces<V, NP>(a, a.part64, a.slot64);
+        fold_pieces<V, NP>(a, part_rz, slot_rz);
         if (!grid_sync(a.bar)) return;
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.n_updates, 1u);
       }
     }
 
     // ---- phase A: Q = K P, partial p'q
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      a.active[par ^ 1] = 0u;
-      if (RU) a.ru_flag[par ^ 1] = 0u;
-    }
+    if (RU && blockIdx.x == 0 && threadIdx.x == 0) a.ru_flag[par ^ 1] = 0u;
     FOR_MY_PIECES(a, {
       bool colact[NP];
 #pragma unroll
@@ -703,8 +862,8 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
           // the same direction P and the new r'z
           double rr64[NP];
           S rzt[NP];
-          seg_totals<NP>(a.part64, a.seg_piece[s], a.seg_piece[s + 1], rr64);
-          seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rzt);
+          seg_totals<NP>(a.slot64, a.seg_slot[s], a.seg_slot[s + 1], rr64);
+          seg_totals<NP>(slot_rz, a.seg_slot[s], a.seg_slot[s + 1], rzt);
 #pragma unroll
           for (int q = 0; q < NP; ++q) {
             if (!(fl[q] && colact[q])) continue;
@@ -741,18 +900,20 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
         }
         if (lane == 0) {
           const int r0 = a.unit_row[u0], r1 = a.unit_row[u1];
-          atomicAdd(&a.work[0], (unsigned long long)(r1 - r0));
-          atomicAdd(&a.work[1], (unsigned long long)(a.indptr[r1] - a.indptr[r0]));
+          w_rows += (unsigned long long)(r1 - r0);
+          w_nnz += (unsigned long long)(a.indptr[r1] - a.indptr[r0]);
         }
       }
       warp_store_partials<NP>(acc, part_pq + (int64_t)p * NP);
     })
+    __syncthreads();
+    fold_pieces<V, NP>(a, part_pq, slot_pq);
     if (!grid_sync(a.bar)) return;
 
     // ---- phase B: alpha, X += alpha P, R -= alpha Q, partial r'r (and r'z for Jacobi)
     FOR_MY_PIECES(a, {
       S pq[NP];
-      seg_totals<NP>(part_pq, a.seg_piece[s], a.seg_piece[s + 1], pq);
+      seg_totals<NP>(slot_pq, a.seg_slot[s], a.seg_slot[s + 1], pq);
       V alpha[NP];
       bool act[NP];
       bool any = false;
@@ -792,13 +953,16 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       warp_store_partials<NP>(rr, part_rr + (int64_t)p * NP);
       if (kDiagPC) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
     })
+    __syncthreads();
+    fold_pieces<V, NP>(a, part_rr, slot_rr);
+    if (kDiagPC) fold_pieces<V, NP>(a, part_rz, slot_rz);
     if (!grid_sync(a.bar)) return;
 
     if constexpr (PC == kPrecTwoLevel) {
       // ---- phases R, G: coarse correction of the new residual
-      coarse_restrict<V, NP>(a, st_cur, false, gw, nw);
+      coarse_restrict<V, NP>(a, st_cur, false);
       if (!grid_sync(a.bar)) return;
-      coarse_solve<V, NP>(a, st_cur, false, gw, nw);
+      coarse_solve<V, NP>(a, st_cur, false);
       if (!grid_sync(a.bar)) return;
     }
 
@@ -814,18 +978,20 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
         if (anyact) factor_first_half<V, NP>(a, u0, u1, acc);
         warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
       })
+      __syncthreads();
+      fold_pieces<V, NP>(a, part_rz, slot_rz);
       if (!grid_sync(a.bar)) return;
     }
 
     // ---- phase C: convergence, beta, P = Z + beta P
     FOR_MY_PIECES(a, {
       S pq[NP], rzn[NP], rr[NP];
-      seg_totals<NP>(part_pq, a.seg_piece[s], a.seg_piece[s + 1], pq);
-      seg_totals<NP>(part_rz, a.seg_piece[s], a.seg_piece[s + 1], rzn);
-      seg_totals<NP>(part_rr, a.seg_piece[s], a.seg_piece[s + 1], rr);
+      seg_totals<NP>(slot_pq, a.seg_slot[s], a.seg_slot[s + 1], pq);
+      seg_totals<NP>(slot_rz, a.seg_slot[s], a.seg_slot[s + 1], rzn);
+      seg_totals<NP>(slot_rr, a.seg_slot[s], a.seg_slot[s + 1], rr);
       if constexpr (PC == kPrecTwoLevel) {
         S c[NP];
-        seg_totals<NP>(a.csl, a.pc.seg_agg[s], a.pc.seg_agg[s + 1], c);
+        seg_totals<NP>(a.aslot, a.pc.seg_aslot[s], a.pc.seg_aslot[s + 1], c);
 #pragma unroll
         for (int q = 0; q < NP; ++q) rzn[q] += c[q];
       }
@@ -857,7 +1023,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
         if (first && lane == q) {
           st_nxt[s * NP + q] = st;
           rz_nxt[s * NP + q] = rzn[q];
-          if (act[q]) atomicAdd(&a.active[par ^ 1], 1u);
+          if (act[q]) s_act = 1;
           if (RU && req) {
             a.ru_col[(par ^ 1) * (int64_t)a.nseg * NP + s * NP + q] = 1;
             atomicOr(&a.ru_flag[par ^ 1], 1u);
@@ -885,7 +1051,9 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
         }
       }
     })
-    if (!grid_sync(a.bar)) return;
+    if (!grid_sync(a.bar, &s_act, &s_seen)) return;
+    nact = s_seen - seen_prev;
+    seen_prev = s_seen;
   }
 
   // ---- publish the final state (the warp holding a segment's first piece)
@@ -913,6 +1081,10 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     }
   })
   if (blockIdx.x == 0 && threadIdx.x == 0) a.iters[0] = it;
+  if (lane == 0 && w_rows != 0) {
+    atomicAdd(&a.work[0], w_rows);
+    atomicAdd(&a.work[1], w_nnz);
+  }
 }
 
 // ---- sliced-ELL construction ---------------------------------------------
@@ -999,14 +1171,19 @@ size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size
   const size_t vec = a256((size_t)n * p * elem_size);
   size_t b = vec * (precond == kPrecFactored ? 4 : 3);  // R P Q (+ T)
   b += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
+  b += a256(sizeof(double) * 3 * (size_t)ct.nslot * p);
+  b += a256(sizeof(double) * (size_t)ct.nslot * p);
   b += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
   b += a256(sizeof(double) * (size_t)ct.nseg * p);
   b += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
-  b += a256(64);  // active[2], iters, barrier, work counters, update flags
+  b += a256(256);  // control words and the barrier word
   // reliable updates: FP64 partials, reference residuals, request flags
   b += a256(sizeof(double) * (size_t)ct.npiece * p) + a256(sizeof(double) * (size_t)ct.nseg * p) +
        a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
-  if (precond == kPrecTwoLevel) b += 3 * a256(sizeof(double) * (size_t)std::max<int64_t>(nagg, 1) * p);
+  if (precond == kPrecTwoLevel) {
+    b += 3 * a256(sizeof(double) * (size_t)std::max<int64_t>(nagg, 1) * p);
+    b += a256(sizeof(double) * (size_t)(nagg + ct.nvc + 1) * p);  // coarse reduction slots
+  }
   return b + 256;
 }
 
@@ -1064,6 +1241,11 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.piece_seg = ct.piece_seg;
   a.vw_piece = ct.vw_piece;
   a.seg_piece = ct.seg_piece;
+  a.vc_piece = ct.vc_piece;
+  a.seg_slot = ct.seg_slot;
+  a.seg_vc0 = ct.seg_vc0;
+  a.nvc = ct.nvc;
+  a.nslot = ct.nslot;
   a.nvw = ct.nvw;
   a.npiece = ct.npiece;
   a.nseg = ct.nseg;
@@ -1079,20 +1261,22 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   }
   using S = ScalarOf<V>;
   a.part = (S*)w; w += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
+  a.slot = (S*)w; w += a256(sizeof(double) * 3 * (size_t)ct.nslot * p);
   a.rz = (S*)w; w += a256(sizeof(double) * 2 * (size_t)ct.nseg * p);
   a.bb = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
   a.state = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
-  unsigned* ctl = (unsigned*)w;  // active[2], iters, count, gen, err, work[2] (u64), ru_flag[2], updates
-  w += a256(64);
-  a.active = ctl;
+  // control words: [2] iters, [5] err, [6..9] work (u64 x2), [10..11] ru_flag,
+  // [12] updates; the barrier word sits alone on the next 128-byte line
+  unsigned* ctl = (unsigned*)w;
+  w += a256(256);
   a.iters = (int*)(ctl + 2);
-  a.bar.count = ctl + 3;
-  a.bar.gen = ctl + 4;
+  a.bar.word = (unsigned long long*)(ctl + 32);
   a.bar.err = (int*)(ctl + 5);
   a.work = (unsigned long long*)(ctl + 6);
   a.ru_flag = ctl + 10;
   a.n_updates = ctl + 12;
   a.part64 = (double*)w; w += a256(sizeof(double) * (size_t)ct.npiece * p);
+  a.slot64 = (double*)w; w += a256(sizeof(double) * (size_t)ct.nslot * p);
   a.rref = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
   a.ru_col = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
   if (pc.kind == kPrecTwoLevel) {
@@ -1100,6 +1284,11 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
     a.rc = (S*)w; w += cb;
     a.yc = (S*)w; w += cb;
     a.csl = (S*)w; w += cb;
+    if ((int64_t)pc.naslot > (int64_t)pc.nagg + ct.nvc + 1) {
+      lapy_set_last_message("pcg: coarse reduction slots exceed the workspace bound");
+      return LAPY_ERR_WORKSPACE;
+    }
+    a.aslot = (S*)w; w += a256(sizeof(double) * (size_t)(pc.nagg + ct.nvc + 1) * p);
   }
   a.state_out = state_dev;
   a.rtol2 = (S)(rtol * rtol);
@@ -1110,7 +1299,13 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.K64 = K64;
   a.delta2 = (S)(delta * delta);
   a.ru_every = std::max(1, ru_every);
-  LAPY_CUDA_TRY(cudaMemsetAsync(ctl, 0, 64, stream));
+  LAPY_CUDA_TRY(cudaMemsetAsync(ctl, 0, 256, stream));
+  // every slot is rewritten by each fold; cleared once so that none is ever
+  // read uninitialised
+  LAPY_CUDA_TRY(cudaMemsetAsync(a.slot, 0, sizeof(double) * 3 * (size_t)ct.nslot * p, stream));
+  if (pc.kind == kPrecTwoLevel)
+    LAPY_CUDA_TRY(cudaMemsetAsync(a.aslot, 0, sizeof(double) * (size_t)std::max(pc.naslot, 1) * p, stream));
+  LAPY_CUDA_TRY(cudaMemsetAsync(a.slot64, 0, sizeof(double) * (size_t)ct.nslot * p, stream));
   if (ru) LAPY_CUDA_TRY(cudaMemsetAsync(a.ru_col, 0, sizeof(int32_t) * 2 * (size_t)ct.nseg * p, stream));
   // segments without rows have no piece: they are reported as solved
   LAPY_CUDA_TRY(cudaMemsetAsync(state_dev, 0, sizeof(int32_t) * (size_t)ct.nseg * p, stream));

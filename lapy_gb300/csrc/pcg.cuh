@@ -28,9 +28,18 @@ struct ChunkTable {
   int32_t* piece_seg = nullptr;   // device, npiece
   int32_t* vw_piece = nullptr;    // device, nvw + 1
   int32_t* seg_piece = nullptr;   // device, nseg + 1
+  // Virtual CTAs: groups of 8 consecutive virtual warps (a CTA's worth).  A
+  // segment's partial sums are folded into one reduction slot per virtual
+  // CTA holding a piece of it: slots [seg_slot[s], seg_slot[s+1]) belong to
+  // the virtual CTAs seg_vc0[s], seg_vc0[s] + 1, ...
+  int nvc = 0, nslot = 0;
+  int32_t* vc_piece = nullptr;    // device, nvc + 1
+  int32_t* seg_slot = nullptr;    // device, nseg + 1
+  int32_t* seg_vc0 = nullptr;     // device, nseg
   std::vector<int32_t> h_seg_row;
   std::vector<int32_t> h_chunk_row, h_chunk_seg, h_seg_chunk;
   std::vector<int32_t> h_unit_row, h_piece_unit, h_piece_seg, h_vw_piece, h_seg_piece;
+  std::vector<int32_t> h_vc_piece, h_seg_slot, h_seg_vc0;
 };
 
 // Plan chunks (and the PCG's warp plan) for the given segments (host);
@@ -88,6 +97,14 @@ struct PcgPrecondDesc {
   const int32_t* seg_agg = nullptr;   // nseg + 1: aggregate range of each segment
   const int64_t* kinv_off = nullptr;  // nseg: offset of the segment's nc x nc inverse
   const float* kinv = nullptr;        // dense (W'KW)^-1 blocks, row-major, FP32
+  // coarse work split over the PCG's virtual CTAs: aggregates
+  // [vc_agg[v], vc_agg[v+1]) (contiguous, about equal cost) go to virtual
+  // CTA v; segment s owns the reduction slots [seg_aslot[s], seg_aslot[s+1])
+  // of the virtual CTAs seg_avc0[s], seg_avc0[s] + 1, ...
+  int nvc = 0, naslot = 0;
+  const int32_t* vc_agg = nullptr;     // nvc + 1
+  const int32_t* seg_aslot = nullptr;  // nseg + 1
+  const int32_t* seg_avc0 = nullptr;   // nseg
 };
 
 // Scratch needed by one persistent PCG solve of n rows x p columns (nagg:
