@@ -381,6 +381,7 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   pc->kinv = d_kinv;
   pc->nvc = nvc;
   pc->naslot = seg_aslot[nseg];
+  pc->max_seg_agg = nseg > 0 ? *std::max_element(nc.begin(), nc.end()) : 0;
   pc->vc_agg = d_vca;
   pc->seg_aslot = d_asl;
   pc->seg_avc0 = d_av0;

@@ -28,6 +28,10 @@ constexpr int kWarps = kPcgThreads / 32;
 constexpr int kUnit = 32;
 constexpr int kStageWarp = 384;   // staged nonzeros per warp (values + column indices)
 constexpr int kPlanCtasPerSm = 5; // resident CTAs per SM the warp plan assumes (48 registers)
+// Partial sums are folded into per-CTA reduction slots when a segment has
+// more pieces, or coarse unknowns, than these.
+constexpr int kFoldPieces = 64;
+constexpr int kFoldAggs = 1024;
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -182,6 +186,7 @@ struct PcgArgs {
   int nseg;
   int nvc;
   int nslot;
+  int fold;  // fold partial sums into reduction slots (segments with many pieces)
   const V* B;
   V* X;
   V* R;
@@ -440,17 +445,42 @@ __device__ __forceinline__ void fold_pieces(const PcgArgs<V>& a, const S* __rest
   }
 }
 
-// Visit the aggregates (coarse unknowns) this warp handles: those of the
-// CTA's virtual CTAs (contiguous ranges of about equal coarse work), every
-// kWarps-th one starting at the warp's index; s is the aggregate's segment.
+// Visit the aggregates (coarse unknowns) this warp handles; s is the
+// aggregate's segment.  Folding launches take those of the CTA's virtual
+// CTAs (contiguous ranges of equal aggregate counts, every kWarps-th one
+// starting at the warp's index), so that their partial sums fold into the
+// CTA's slots; the others deal all aggregates round-robin over all warps.
 #define FOR_MY_AGGS(a, ...)                                                                 \
-  for (int vc = blockIdx.x; vc < (a).pc.nvc; vc += gridDim.x) {                            \
-    for (int g = (a).pc.vc_agg[vc] + (int)(threadIdx.x >> 5); g < (a).pc.vc_agg[vc + 1];   \
-         g += kWarps) {                                                                    \
+  if ((a).fold) {                                                                          \
+    for (int vc = blockIdx.x; vc < (a).pc.nvc; vc += gridDim.x) {                          \
+      for (int g = (a).pc.vc_agg[vc] + (int)(threadIdx.x >> 5); g < (a).pc.vc_agg[vc + 1]; \
+           g += kWarps) {                                                                  \
+        const int s = (a).pc.agg_sid[g];                                                   \
+        __VA_ARGS__                                                                        \
+      }                                                                                    \
+    }                                                                                      \
+  } else {                                                                                 \
+    for (int g = blockIdx.x * kWarps + (int)(threadIdx.x >> 5); g < (a).pc.nagg;           \
+         g += gridDim.x * kWarps) {                                                        \
       const int s = (a).pc.agg_sid[g];                                                     \
       __VA_ARGS__                                                                          \
     }                                                                                      \
   }
+
+// Column totals of segment s: from its reduction slots when the launch
+// folds, else straight from the partial sums of its pieces (of its
+// aggregates, for the coarse term).
+template <typename V, int NP, typename S>
+__device__ __forceinline__ void piece_totals(const PcgArgs<V>& a, const S* __restrict__ part,
+                                             const S* __restrict__ slots, int s, S (&tot)[NP]) {
+  if (a.fold) seg_totals<NP>(slots, a.seg_slot[s], a.seg_slot[s + 1], tot);
+  else seg_totals<NP>(part, a.seg_piece[s], a.seg_piece[s + 1], tot);
+}
+template <typename V, int NP, typename S>
+__device__ __forceinline__ void coarse_totals(const PcgArgs<V>& a, int s, S (&tot)[NP]) {
+  if (a.fold) seg_totals<NP>(a.aslot, a.pc.seg_aslot[s], a.pc.seg_aslot[s + 1], tot);
+  else seg_totals<NP>(a.csl, a.pc.seg_agg[s], a.pc.seg_agg[s + 1], tot);
+}
 
 // Fold the per-aggregate csl values of the CTA's virtual CTAs into one slot
 // per (segment, virtual CTA), one warp per segment (after a __syncthreads).
@@ -540,8 +570,10 @@ __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t*
       }
     }
   })
-  __syncthreads();
-  fold_aggs<V, NP>(a, a.csl, a.aslot);
+  if (a.fold) {
+    __syncthreads();
+    fold_aggs<V, NP>(a, a.csl, a.aslot);
+  }
 }
 
 // z = dinv .* r (+ the coarse correction W yc for the two-level preconditioner)
@@ -678,9 +710,11 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     warp_store_partials<NP>(bb, part_rr + (int64_t)p * NP);
     if (kDiagPC) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
   })
-  __syncthreads();
-  fold_pieces<V, NP>(a, part_rr, slot_rr);
-  if (kDiagPC) fold_pieces<V, NP>(a, part_rz, slot_rz);
+  if (a.fold) {
+    __syncthreads();
+    fold_pieces<V, NP>(a, part_rr, slot_rr);
+    if (kDiagPC) fold_pieces<V, NP>(a, part_rz, slot_rz);
+  }
   if constexpr (PC == kPrecTwoLevel) {
     if (!grid_sync(a.bar)) return;
     coarse_restrict<V, NP>(a, nullptr, true);
@@ -696,8 +730,10 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       factor_first_half<V, NP>(a, u0, u1, acc);
       warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
     })
-    __syncthreads();
-    fold_pieces<V, NP>(a, part_rz, slot_rz);
+    if (a.fold) {
+      __syncthreads();
+      fold_pieces<V, NP>(a, part_rz, slot_rz);
+    }
   }
   if (!grid_sync(a.bar)) return;
   // ---- segment initialisation (the warp holding a segment's first piece publishes)
@@ -724,11 +760,11 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     }
     if (a.seg_piece[s] == p) {
       S bb[NP], rz[NP];
-      seg_totals<NP>(slot_rr, a.seg_slot[s], a.seg_slot[s + 1], bb);
-      seg_totals<NP>(slot_rz, a.seg_slot[s], a.seg_slot[s + 1], rz);
+      piece_totals<V, NP>(a, part_rr, slot_rr, s, bb);
+      piece_totals<V, NP>(a, part_rz, slot_rz, s, rz);
       if constexpr (PC == kPrecTwoLevel) {
         S c[NP];
-        seg_totals<NP>(a.aslot, a.pc.seg_aslot[s], a.pc.seg_aslot[s + 1], c);
+        coarse_totals<V, NP>(a, s, c);
 #pragma unroll
         for (int q = 0; q < NP; ++q) rz[q] += c[q];
       }
@@ -836,9 +872,11 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
           warp_store_partials<NP>(rr, a.part64 + (int64_t)p * NP);
           warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
         })
-        __syncthreads();
-        fold_pieces<V, NP>(a, a.part64, a.slot64);
-        fold_pieces<V, NP>(a, part_rz, slot_rz);
+        if (a.fold) {
+          __syncthreads();
+          fold_pieces<V, NP>(a, a.part64, a.slot64);
+          fold_pieces<V, NP>(a, part_rz, slot_rz);
+        }
         if (!grid_sync(a.bar)) return;
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.n_updates, 1u);
       }
@@ -862,8 +900,8 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
           // the same direction P and the new r'z
           double rr64[NP];
           S rzt[NP];
-          seg_totals<NP>(a.slot64, a.seg_slot[s], a.seg_slot[s + 1], rr64);
-          seg_totals<NP>(slot_rz, a.seg_slot[s], a.seg_slot[s + 1], rzt);
+          piece_totals<V, NP>(a, a.part64, a.slot64, s, rr64);
+          piece_totals<V, NP>(a, part_rz, slot_rz, s, rzt);
 #pragma unroll
           for (int q = 0; q < NP; ++q) {
             if (!(fl[q] && colact[q])) continue;
@@ -906,14 +944,16 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       }
       warp_store_partials<NP>(acc, part_pq + (int64_t)p * NP);
     })
-    __syncthreads();
-    fold_pieces<V, NP>(a, part_pq, slot_pq);
+    if (a.fold) {
+      __syncthreads();
+      fold_pieces<V, NP>(a, part_pq, slot_pq);
+    }
     if (!grid_sync(a.bar)) return;
 
     // ---- phase B: alpha, X += alpha P, R -= alpha Q, partial r'r (and r'z for Jacobi)
     FOR_MY_PIECES(a, {
       S pq[NP];
-      seg_totals<NP>(slot_pq, a.seg_slot[s], a.seg_slot[s + 1], pq);
+      piece_totals<V, NP>(a, part_pq, slot_pq, s, pq);
       V alpha[NP];
       bool act[NP];
       bool any = false;
@@ -953,9 +993,11 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       warp_store_partials<NP>(rr, part_rr + (int64_t)p * NP);
       if (kDiagPC) warp_store_partials<NP>(rz, part_rz + (int64_t)p * NP);
     })
-    __syncthreads();
-    fold_pieces<V, NP>(a, part_rr, slot_rr);
-    if (kDiagPC) fold_pieces<V, NP>(a, part_rz, slot_rz);
+    if (a.fold) {
+      __syncthreads();
+      fold_pieces<V, NP>(a, part_rr, slot_rr);
+      if (kDiagPC) fold_pieces<V, NP>(a, part_rz, slot_rz);
+    }
     if (!grid_sync(a.bar)) return;
 
     if constexpr (PC == kPrecTwoLevel) {
@@ -978,20 +1020,22 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
         if (anyact) factor_first_half<V, NP>(a, u0, u1, acc);
         warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
       })
-      __syncthreads();
-      fold_pieces<V, NP>(a, part_rz, slot_rz);
+      if (a.fold) {
+        __syncthreads();
+        fold_pieces<V, NP>(a, part_rz, slot_rz);
+      }
       if (!grid_sync(a.bar)) return;
     }
 
     // ---- phase C: convergence, beta, P = Z + beta P
     FOR_MY_PIECES(a, {
       S pq[NP], rzn[NP], rr[NP];
-      seg_totals<NP>(slot_pq, a.seg_slot[s], a.seg_slot[s + 1], pq);
-      seg_totals<NP>(slot_rz, a.seg_slot[s], a.seg_slot[s + 1], rzn);
-      seg_totals<NP>(slot_rr, a.seg_slot[s], a.seg_slot[s + 1], rr);
+      piece_totals<V, NP>(a, part_pq, slot_pq, s, pq);
+      piece_totals<V, NP>(a, part_rz, slot_rz, s, rzn);
+      piece_totals<V, NP>(a, part_rr, slot_rr, s, rr);
       if constexpr (PC == kPrecTwoLevel) {
         S c[NP];
-        seg_totals<NP>(a.aslot, a.pc.seg_aslot[s], a.pc.seg_aslot[s + 1], c);
+        coarse_totals<V, NP>(a, s, c);
 #pragma unroll
         for (int q = 0; q < NP; ++q) rzn[q] += c[q];
       }
@@ -1246,6 +1290,13 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.seg_vc0 = ct.seg_vc0;
   a.nvc = ct.nvc;
   a.nslot = ct.nslot;
+  {
+    // fold into reduction slots only when some segment has many pieces (or
+    // coarse unknowns): with few, the direct sums are cheaper
+    int maxp = 0;
+    for (int s = 0; s < ct.nseg; ++s) maxp = std::max(maxp, ct.h_seg_piece[s + 1] - ct.h_seg_piece[s]);
+    a.fold = (maxp > kFoldPieces || (pc.kind == kPrecTwoLevel && pc.max_seg_agg > kFoldAggs)) ? 1 : 0;
+  }
   a.nvw = ct.nvw;
   a.npiece = ct.npiece;
   a.nseg = ct.nseg;

@@ -101,7 +101,7 @@ struct PcgPrecondDesc {
   // [vc_agg[v], vc_agg[v+1]) (contiguous, about equal cost) go to virtual
   // CTA v; segment s owns the reduction slots [seg_aslot[s], seg_aslot[s+1])
   // of the virtual CTAs seg_avc0[s], seg_avc0[s] + 1, ...
-  int nvc = 0, naslot = 0;
+  int nvc = 0, naslot = 0, max_seg_agg = 0;
   const int32_t* vc_agg = nullptr;     // nvc + 1
   const int32_t* seg_aslot = nullptr;  // nseg + 1
   const int32_t* seg_avc0 = nullptr;   // nseg
