@@ -387,9 +387,9 @@ def run_plain_spectra(args, meshes, lv, batched_per_gpu):
 def _single_mesh(args):
     from lapy_gb300 import meshes
 
-    if args.workload == "c1":
+    if args.workload == "sphere-l5":
         return meshes.icosphere(5)
-    if args.workload == "c2":
+    if args.workload == "kuhn-64":
         return meshes.kuhn_cube(64, jitter=0.2, seed=args.seed)
     return meshes.deformed_icospheres([8], [args.seed])[0]
 
@@ -417,10 +417,10 @@ def _cpu_single(workload, v, t, seed):
     import oracle
 
     t0 = time.perf_counter()
-    if workload == "c1":
+    if workload == "sphere-l5":
         A, M = oracle.assemble_scipy(v, t)
         oracle.eigs(A, M, k=50)
-    elif workload == "c2":
+    elif workload == "kuhn-64":
         from scipy.sparse.linalg import splu
 
         A, M = oracle.assemble_scipy(v, t)
@@ -455,23 +455,24 @@ def cpu_single(workload, mesh, seed, timeout):
 
 
 def run_single(args):
-    """C1 (icosphere L5, eigs 50), C2 (Kuhn 64^3 tets: eigs 100 + 10 heat steps),
-    C3 (deformed icosphere L8: heat + heat-method geodesics), from host arrays
+    """sphere-l5 (icosphere L5, eigs 50), kuhn-64 (Kuhn 64^3 tets: eigs 100 + 10
+    heat steps), sphere-l8-geodesics (deformed icosphere L8: heat + heat-method
+    geodesics), from host arrays
     through the public API each step (so value and e2e coincide)."""
     import torch
 
     from lapy_gb300 import Solver, TetMesh, TriaMesh, diffgeo, heat
 
     mesh0 = _single_mesh(args)
-    cls = TetMesh if args.workload == "c2" else TriaMesh
+    cls = TetMesh if args.workload == "kuhn-64" else TriaMesh
     info = {}
 
     def step():
         mesh = cls(mesh0.v.copy(), mesh0.t.copy())  # fresh upload every step
-        if args.workload == "c1":
+        if args.workload == "sphere-l5":
             ev, _ = Solver(mesh, lump=False).eigs(k=50)
             info["ev"] = ev
-        elif args.workload == "c2":
+        elif args.workload == "kuhn-64":
             fem = Solver(mesh, lump=False)
             ev, _ = fem.eigs(k=100)
             u = _c2_heat_steps(fem, mesh)
@@ -490,9 +491,9 @@ def run_single(args):
         for _ in range(args.steps):
             step()
         wall = time.perf_counter() - t0
-    names = {"c1": ("k=50 spectra/s (icosphere L5, 10,242 vertices)", "spectra/s"),
-             "c2": ("C2 runs/s (Kuhn 64^3 tets: eigs(100) + 10 heat steps)", "runs/s"),
-             "c3": ("C3 runs/s (deformed icosphere L8: heat + geodesics)", "runs/s")}
+    names = {"sphere-l5": ("k=50 spectra/s (icosphere L5, 10,242 vertices)", "spectra/s"),
+             "kuhn-64": ("runs/s (Kuhn 64^3 tets: eigs(100) + 10 heat steps)", "runs/s"),
+             "sphere-l8-geodesics": ("runs/s (deformed icosphere L8: heat + geodesics)", "runs/s")}
     metric, unit = names[args.workload]
     v = args.steps / wall
     line = {"metric": metric, "value": v, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -500,7 +501,7 @@ def run_single(args):
             "dtype": "f32 inner PCG / f64 Lanczos and refinement", "data": "synthetic",
             "config": {"workload": args.workload, "vertices": int(len(mesh0.v)), "elements": int(len(mesh0.t))},
             "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": int(mesh0.v.nbytes + mesh0.t.size * 4),
-                    "d2h_bytes_per_step": int(8 * (50 if args.workload == "c1" else len(mesh0.v)))},
+                    "d2h_bytes_per_step": int(8 * (50 if args.workload == "sphere-l5" else len(mesh0.v)))},
             "clocks": clk.summary(), "check": {k: (float(np.asarray(x).ravel()[-1]) if k == "ev" else x)
                                                for k, x in info.items()}}
     if not args.no_cpu:
@@ -538,8 +539,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="shapedna", choices=["shapedna", "c1", "c2", "c3"],
-                    help="shapedna: the batched headline (512 meshes); c1-c3: single-mesh configurations")
+    ap.add_argument("--workload", default="shapedna", choices=["shapedna", "sphere-l5", "kuhn-64", "sphere-l8-geodesics"],
+                    help="shapedna: the batched headline (512 meshes); the others: single-mesh workloads")
     ap.add_argument("--meshes", type=int, default=512)
     ap.add_argument("--block", type=int, default=4)
     ap.add_argument("--seed", type=int, default=2024)

@@ -34,6 +34,52 @@ def compute_shapedna(geom, k: int = 50, lump: bool = False, aniso=None, aniso_sm
     return _ev_dict(geom, k, evals, evecs)
 
 
+def _positive_measure(value: float, name: str) -> float:
+    if value <= 0:
+        raise ValueError(f"{name} must be positive for normalization")
+    return value
+
+
+def normalize_ev(geom, evals: np.ndarray, method: str = "geometry") -> np.ndarray:
+    """Eigenvalues scaled to unit surface area ('surface'), unit volume
+    ('volume': the enclosed volume of a closed triangle mesh, or of a
+    tetrahedral mesh's boundary, to the power 2/3) or by the mesh type
+    ('geometry': surface for triangles, volume for tetrahedra), as
+    lapy/shapedna.py:169-227.  Host arithmetic on the k eigenvalues; the
+    measures are O(m) host sums."""
+    geom_type = type(geom).__name__
+    if method == "surface":
+        return evals * _positive_measure(geom.area(), "area")
+    if method == "volume":
+        if geom_type == "TriaMesh":
+            return evals * _positive_measure(geom.volume(), "volume") ** (2.0 / 3.0)
+        if geom_type == "TetMesh":
+            return evals * _positive_measure(geom.boundary_volume(), "boundary volume") ** (2.0 / 3.0)
+        raise ValueError("Unsupported geometry type for volume normalization")
+    if method == "geometry":
+        if geom_type == "TriaMesh":
+            return evals * _positive_measure(geom.area(), "area")
+        if geom_type == "TetMesh":
+            return evals * _positive_measure(geom.boundary_volume(), "boundary volume") ** (2.0 / 3.0)
+        raise ValueError("Unsupported geometry type for geometry normalization")
+    raise ValueError(f"Unknown normalization method: {method}")
+
+
+def reweight_ev(evals: np.ndarray) -> np.ndarray:
+    """Eigenvalue i (0-based) divided by i + 1 (lapy/shapedna.py:230-255)."""
+    return evals / np.arange(1, len(evals) + 1)
+
+
+def compute_distance(ev1: np.ndarray, ev2: np.ndarray, dist: str = "euc") -> float:
+    """Euclidean distance of two spectra; other measures raise ValueError as
+    in lapy/shapedna.py:258-295."""
+    if dist != "euc":
+        raise ValueError(f"Distance metric {dist} is not implemented.")
+    from scipy.spatial import distance
+
+    return distance.euclidean(ev1, ev2)
+
+
 class BatchInput:
     """Meshes of one element type concatenated on the device.
 

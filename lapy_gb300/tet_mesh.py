@@ -24,3 +24,21 @@ class TetMesh:
         from ._geometry import avg_edge_length
 
         return avg_edge_length(self)
+
+    def boundary_volume(self) -> float:
+        """Volume enclosed by the boundary surface: the faces that belong to a
+        single tetrahedron, each oriented away from its tetrahedron, summed as
+        signed volumes with the origin.  This is the measure ShapeDNA
+        normalises by (lapy/shapedna.py:50-70: the boundary mesh, oriented,
+        then its volume); host, O(m)."""
+        t = np.asarray(self.t)
+        p = [self.v[t[:, i], :] for i in range(4)]
+        flip = np.sum(np.cross(p[1] - p[0], p[2] - p[0]) * (p[3] - p[0]), axis=1) < 0
+        # faces opposite vertex 0, 1, 2, 3, outward for a positive tetrahedron
+        faces = np.vstack([t[:, [3, 1, 2]], t[:, [2, 0, 3]], t[:, [1, 3, 0]], t[:, [0, 2, 1]]])
+        fl = np.tile(flip, 4)
+        faces[fl] = faces[fl][:, [0, 2, 1]]
+        _, inv, cnt = np.unique(np.sort(faces, axis=1), axis=0, return_inverse=True, return_counts=True)
+        bnd = faces[cnt[inv.ravel()] == 1]
+        q0, q1, q2 = (self.v[bnd[:, i], :] for i in range(3))
+        return np.sum(np.sum(q0 * np.cross(q1 - q0, q2 - q0), axis=1)) / 6.0

@@ -59,6 +59,48 @@ class TriaMesh:
 
         return avg_edge_length(self)
 
+    # -- measures used to normalise spectra (host, O(m)) -------------------
+    def _edge_counts(self, directed: bool) -> np.ndarray:
+        e = np.concatenate([self.t[:, [0, 1]], self.t[:, [1, 2]], self.t[:, [2, 0]]])
+        if not directed:
+            e = np.sort(e, axis=1)
+        return np.unique(e, axis=0, return_counts=True)[1]
+
+    def is_closed(self) -> bool:
+        """No boundary edge: every edge lies in two or more triangles
+        (lapy/tria_mesh.py:562-572)."""
+        return not np.any(self._edge_counts(directed=False) == 1)
+
+    def is_oriented(self) -> bool:
+        """Consistent orientation: no directed edge is used twice
+        (lapy/tria_mesh.py:604-616)."""
+        return int(self._edge_counts(directed=True).max()) == 1
+
+    def tria_areas(self) -> np.ndarray:
+        """Triangle areas by Heron's formula from the three edge lengths
+        (lapy/tria_mesh.py:636-658)."""
+        p0, p1, p2 = (self.v[self.t[:, i], :] for i in range(3))
+        a = np.sqrt(np.sum((p1 - p0) ** 2, axis=1))
+        b = np.sqrt(np.sum((p2 - p1) ** 2, axis=1))
+        c = np.sqrt(np.sum((p0 - p2) ** 2, axis=1))
+        s = 0.5 * (a + b + c)
+        return np.sqrt(s * (s - a) * (s - b) * (s - c))
+
+    def area(self) -> float:
+        """Total surface area (lapy/tria_mesh.py:660-669)."""
+        return np.sum(self.tria_areas())
+
+    def volume(self) -> float:
+        """Volume enclosed by a closed, oriented mesh: the signed volumes of
+        the tetrahedra the triangles span with the origin
+        (lapy/tria_mesh.py:671-703)."""
+        if not self.is_closed():
+            raise ValueError("Mesh must be closed to compute volume.")
+        if not self.is_oriented():
+            raise ValueError("Mesh must be oriented to compute volume.")
+        p0, p1, p2 = (self.v[self.t[:, i], :] for i in range(3))
+        return np.sum(np.sum(p0 * np.cross(p1 - p0, p2 - p0), axis=1)) / 6.0
+
     def refine_(self, it: int = 1) -> None:
         """1-to-4 midpoint subdivision (lapy/tria_mesh.py:1452-1487).
 

@@ -151,7 +151,7 @@ def test_eigs_tet_kuhn(cuda_ok):
 
 
 def test_eigs_deformed_l5_k50_against_eigsh(cuda_ok):
-    """C1-sized (10,242 vertices) deformed sphere, k=50 vs the reference method (eigsh + splu)."""
+    """Icosphere-L5-sized (10,242 vertices) deformed sphere, k=50 vs the reference method (eigsh + splu)."""
     from lapy_gb300 import Solver, meshes
 
     mesh = meshes.sh_deform(meshes.icosphere(5), seed=21)
