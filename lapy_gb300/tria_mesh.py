@@ -90,6 +90,24 @@ class TriaMesh:
         """Total surface area (lapy/tria_mesh.py:660-669)."""
         return np.sum(self.tria_areas())
 
+    def centroid(self) -> tuple[np.ndarray, float]:
+        """Area-weighted mean of the triangle centres, and the total area
+        (lapy/tria_mesh.py:990-1015)."""
+        p0, p1, p2 = (self.v[self.t[:, i], :] for i in range(3))
+        cr = np.cross(p2 - p1, p0 - p2)
+        areas = 0.5 * np.sqrt(np.sum(cr * cr, axis=1))
+        total = areas.sum()
+        w = areas / total
+        return np.sum(((p0 + p1 + p2) / 3.0) * w[:, np.newaxis], axis=0), total
+
+    def normalize_(self) -> None:
+        """Centroid to the origin, then scale to unit surface area
+        (lapy/tria_mesh.py:1390-1405)."""
+        c, area = self.centroid()
+        if area <= 0:
+            raise ValueError("Mesh surface area must be positive to normalize.")
+        self.v = (1.0 / np.sqrt(area)) * (self.v - c)
+
     def volume(self) -> float:
         """Volume enclosed by a closed, oriented mesh: the signed volumes of
         the tetrahedra the triangles span with the origin

@@ -336,6 +336,36 @@ def geodesic_f(v, t, u, scaled=True, consistent=False):
     return x - x.min(axis=0)
 
 
+def _normalize_tria(v, t):
+    """Centroid (area-weighted triangle centres) to the origin, unit area
+    (tria_mesh.py:990-1015, 1390-1405)."""
+    p0, p1, p2 = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+    cr = np.cross(p2 - p1, p0 - p2)
+    areas = 0.5 * np.sqrt(np.sum(cr * cr, axis=1))
+    total = areas.sum()
+    c = np.sum(((p0 + p1 + p2) / 3.0) * (areas / total)[:, None], axis=0)
+    return (1.0 / np.sqrt(total)) * (v - c)
+
+
+def mean_curvature_flow(v, t, max_iter=30, stop_eps=1e-13, step=1.0):
+    """tria_mean_curvature_flow (diffgeo.py:523-606): fixed stiffness of the
+    normalised mesh, lumped mass of the current mesh, (M + step A) V = M V by
+    a sparse LU, re-normalise, stop on sum_k (dv_k' M dv_k)^2 < stop_eps."""
+    from scipy.sparse.linalg import spsolve
+
+    v = _normalize_tria(np.asarray(v), t)
+    A, _ = assemble_scipy(v, t, lump=True)
+    for _ in range(max_iter):
+        v_last = v
+        _, M = assemble_scipy(v, t, lump=True)
+        v = spsolve(sparse.csc_matrix(M + step * A), M @ v)
+        v = _normalize_tria(v, t)
+        dv = v - v_last
+        if np.trace(np.square(dv.T @ (M @ dv))) < stop_eps:
+            break
+    return v
+
+
 __all__ = ["tria_local", "tet_local", "assemble_scipy", "assemble_sorted", "csr_sorted_sum", "avg_edge_length",
            "eigs", "eigs_dense", "poisson", "diffusion", "tria_gradient", "tet_gradient", "tria_divergence", "tet_divergence",
-           "normalize_rows", "geodesic_f", "poisson_neumann_consistent", "TRIA_IJ", "TET_IJ"]
+           "normalize_rows", "geodesic_f", "poisson_neumann_consistent", "mean_curvature_flow", "TRIA_IJ", "TET_IJ"]
