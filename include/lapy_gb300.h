@@ -152,6 +152,15 @@ int lapy_csr_spmm_f32(int64_t n, const int32_t* indptr, const int32_t* indices,
 int lapy_diag_mm_f64(int64_t n, const double* d, int ncol, const double* x, double* y,
                      double alpha, double beta, void* stream);
 
+/* ---- heat kernel products (lapy/heat.py:19-111) ------------------------
+ * H (nrows x nt, row-major) = W S, W row r = evecs[rows[r], 0:nev] (rows NULL:
+ * row r), squared element-wise when `squared` (the diagonal K(t, x, x));
+ * evecs row-major with leading dimension ld >= nev; S (nev x nt, row-major)
+ * the exp(-lambda t) factors.  Replaces the final np.matmul of heat.diagonal
+ * (heat.py:59) and heat.kernel (heat.py:108). */
+int lapy_heat_product_f64(int64_t nrows, const int64_t* rows, const double* evecs, int64_t ld, int nev,
+                          int squared, const double* S, int nt, double* H, void* stream);
+
 /* ---- element-wise helpers ----------------------------------------------
  * out = a*x + b*y (y may be NULL).  Forms hmat = M + t*A (lapy/heat.py:208)
  * and A - sigma*M (lapy/solver.py:707) on a shared pattern. */

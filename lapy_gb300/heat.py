@@ -1,9 +1,11 @@
-"""GPU drop-in for ``lapy.heat.diffusion`` (lapy/heat.py:114-232).
+"""GPU drop-in for ``lapy.heat`` (lapy/heat.py).
 
-One backward-Euler step ``(M + t A) u = M u0`` with lumped ``M`` and
-``t = m * avg_edge_length**2``, for one or several seed sets; the system is
-solved by FP32 Jacobi-PCG inside FP64 iterative refinement instead of a sparse
-LU factorisation.
+``diffusion`` (heat.py:114-232): one backward-Euler step ``(M + t A) u = M
+u0`` with lumped ``M`` and ``t = m * avg_edge_length**2``, for one or several
+seed sets; the system is solved by FP32 Jacobi-PCG inside FP64 iterative
+refinement instead of a sparse LU factorisation.  ``diagonal`` and ``kernel``
+(heat.py:19-111): heat-kernel values from eigenpairs, the product over the
+mesh's rows by a CUDA kernel.
 """
 
 from __future__ import annotations
@@ -14,9 +16,65 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._device import axpby, dptr, pcg_solve, stream
+from ._device import axpby, dptr, pcg_solve, require_cuda, stream
 
 logger = logging.getLogger(__name__)
+
+
+def _heat_product(evecs, sel, n: int, S, squared: bool) -> np.ndarray:
+    """``np.matmul(W, S)`` for W = evecs[sel, 0:n] (squared element-wise when
+    ``squared``), computed by the GPU product kernel.  ``sel`` holds row
+    indices (any shape); S is the 1-D or 2-D factor the reference forms on the
+    host.  Shapes follow np.matmul, and so do its errors (checked on empty
+    stand-ins before any transfer)."""
+    S = np.asarray(S, dtype=np.float64)
+    w_shape = sel.shape + (n,)
+    # numpy's own shape check on zero-strided stand-ins (no data, no product)
+    stand_w = np.lib.stride_tricks.as_strided(np.zeros(1), shape=(1, n) if len(w_shape) > 1 else (n,),
+                                              strides=(0, 0) if len(w_shape) > 1 else (0,))
+    np.matmul(stand_w, np.zeros(S.shape))
+    if S.ndim not in (1, 2):
+        raise ValueError("the exp(-lambda t) factor must be 1-D or 2-D")
+    out_shape = sel.shape + (S.shape[1],) if S.ndim == 2 else sel.shape
+    nt = S.shape[1] if S.ndim == 2 else 1
+    require_cuda()
+    ev = np.asarray(evecs, dtype=np.float64)
+    ev_d = torch.from_numpy(np.ascontiguousarray(ev)).to("cuda")
+    rows = torch.from_numpy(np.ascontiguousarray(sel.reshape(-1), dtype=np.int64)).to("cuda")
+    s_d = torch.from_numpy(np.ascontiguousarray(S.reshape(n, nt))).to("cuda")
+    h = torch.empty((rows.numel(), nt), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().lapy_heat_product_f64(rows.numel(), dptr(rows), dptr(ev_d), ev.shape[1], n, int(squared),
+                                                 dptr(s_d), nt, dptr(h), stream()), "heat_product")
+    res = h.cpu().numpy().reshape(out_shape)
+    return res[()] if res.ndim == 0 else res
+
+
+def diagonal(t, x, evecs, evals, n: int) -> np.ndarray:
+    """Heat kernel diagonal K(t, x, x) from the first n eigenpairs
+    (lapy/heat.py:19-60): ``evecs[x, :n]**2 @ exp(-evals[:n] @ t)``.  The
+    exponent matrix is formed on the host exactly as the reference does (so
+    ``evals`` as a column and ``t`` as a row give one column per time); the
+    product over the mesh's rows runs on the GPU."""
+    evecs = np.asarray(evecs)
+    evals = np.asarray(evals)
+    if n > evecs.shape[1] or n > evals.shape[0]:
+        raise ValueError("n exceeds the number of available eigenpairs")
+    S = np.exp(-np.matmul(evals[0:n], t))
+    sel = np.arange(evecs.shape[0])[x]
+    return _heat_product(evecs, np.asarray(sel), n, S, squared=True)
+
+
+def kernel(t, vfix: int, evecs, evals, n: int) -> np.ndarray:
+    """Heat kernel K_t(p, vfix) for all p from the first n eigenpairs
+    (lapy/heat.py:63-111): ``evecs[:, :n] @ (exp(-evals[:n] @ t) *
+    evecs[vfix, :n])``, the factor formed on the host with the reference's
+    broadcasting, the product on the GPU."""
+    evecs = np.asarray(evecs)
+    evals = np.asarray(evals)
+    if n > evecs.shape[1] or n > evals.shape[0]:
+        raise ValueError("n exceeds the number of available eigenpairs")
+    S = np.exp(np.matmul(-evals[0:n], t)) * evecs[vfix, 0:n]
+    return _heat_product(evecs, np.arange(evecs.shape[0]), n, S, squared=False)
 
 
 def diffusion(geometry, vids, m: float = 1.0, aniso=None, use_cholmod: bool = False, rtol: float = 1e-11,

@@ -1,6 +1,7 @@
 """Generate tests/golden/ref_post.npz from the reference itself: ShapeDNA
-post-processing (normalize_ev, reweight_ev, compute_distance) and the .ev /
-PSOL text formats (write_ev, write_vfunc, read_ev, read_vfunc).
+post-processing (normalize_ev, reweight_ev, compute_distance), the .ev /
+PSOL text formats (write_ev, write_vfunc, read_ev, read_vfunc) and the heat
+kernel values of lapy.heat (diagonal, kernel).
 
 Runs only where the reference is available:
 
@@ -93,6 +94,18 @@ def main():
             (tmp / f"{key}.psol").write_text(text)
             out[f"vfunc_text_{key}"] = np.array(text)
             out[f"vfunc_read_{key}"] = np.array(rio.read_vfunc(str(tmp / f"{key}.psol")))
+    # heat kernel values from eigenpairs (evals as a column, times as a row)
+    import lapy.heat as rheat
+
+    f = np.load(HERE / "ref_deformed3.npz")
+    ev, evec = f["evals"], f["evecs"]
+    out["hk_evals"], out["hk_evecs"] = ev, evec
+    out["hk_t3"] = np.array([[0.1, 1.0, 5.0]])
+    out["hk_x"] = np.arange(0, len(evec), 7)
+    out["hk_diag_rows"] = rheat.diagonal(out["hk_t3"], out["hk_x"], evec, ev[:, None], 8)
+    out["hk_diag_one"] = rheat.diagonal(out["hk_t3"], 5, evec, ev[:, None], 8)
+    out["hk_kernel_n3"] = rheat.kernel(np.array([[0.2, 0.7, 3.0]]), 3, evec, ev[:, None], 3)
+    out["hk_kernel_t1"] = rheat.kernel(np.array([[0.5]]), 11, evec, ev[:, None], 6)
     np.savez_compressed(HERE / "ref_post.npz", **out)
     print("wrote", HERE / "ref_post.npz", len(out), "entries")
 

@@ -1,8 +1,8 @@
-"""ShapeDNA post-processing and the .ev / PSOL text formats against the
-reference's own outputs (tests/golden/ref_post.npz, made by
-tests/golden/make_golden_post.py): normalize_ev, reweight_ev,
-compute_distance, write_ev / read_ev, write_vfunc / read_vfunc.  Host code
-only: no GPU needed."""
+"""ShapeDNA post-processing, the .ev / PSOL text formats and the heat kernel
+values against the reference's own outputs (tests/golden/ref_post.npz, made
+by tests/golden/make_golden_post.py): normalize_ev, reweight_ev,
+compute_distance, write_ev / read_ev, write_vfunc / read_vfunc (host code),
+heat.diagonal / heat.kernel (GPU product; argument checks on the host)."""
 
 from __future__ import annotations
 
@@ -136,3 +136,36 @@ def test_vfunc_roundtrip(post, tmp_path):
     p.write_text("Solution:\n\n")
     with pytest.raises(ValueError, match="No vertex function"):
         io.read_vfunc(str(p))
+
+
+def test_heat_kernel_argument_errors(post):
+    """Checks that run before any device work (no GPU needed)."""
+    from lapy_gb300 import heat
+
+    ev, evec = post["hk_evals"], post["hk_evecs"]
+    with pytest.raises(ValueError, match="exceeds"):
+        heat.diagonal(post["hk_t3"], post["hk_x"], evec, ev[:, None], evec.shape[1] + 1)
+    with pytest.raises(ValueError, match="exceeds"):
+        heat.kernel(post["hk_t3"], 0, evec, ev[:, None], evec.shape[1] + 1)
+    # a scalar time with 1-D eigenvalues: np.matmul rejects it, as in the reference
+    with pytest.raises(ValueError):
+        heat.diagonal(0.5, post["hk_x"], evec, ev, 4)
+    # times as a row that does not broadcast against the n eigenvector entries
+    with pytest.raises(ValueError):
+        heat.kernel(np.array([[0.1, 0.2]]), 0, evec, ev[:, None], 3)
+
+
+@pytest.mark.gpu
+def test_heat_kernel_gpu_matches_reference(cuda_ok, post):
+    from lapy_gb300 import heat
+
+    ev, evec = post["hk_evals"], post["hk_evecs"]
+    cases = [
+        (heat.diagonal(post["hk_t3"], post["hk_x"], evec, ev[:, None], 8), post["hk_diag_rows"]),
+        (heat.diagonal(post["hk_t3"], 5, evec, ev[:, None], 8), post["hk_diag_one"]),
+        (heat.kernel(np.array([[0.2, 0.7, 3.0]]), 3, evec, ev[:, None], 3), post["hk_kernel_n3"]),
+        (heat.kernel(np.array([[0.5]]), 11, evec, ev[:, None], 6), post["hk_kernel_t1"]),
+    ]
+    for got, want in cases:
+        assert got.shape == want.shape
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-14 * np.abs(want).max())
