@@ -19,6 +19,22 @@ class TetMesh:
         if np.max(self.t) >= vnum:
             raise ValueError("Max index exceeds number of vertices")
 
+    @classmethod
+    def read_vtk(cls, filename: str) -> "TetMesh":
+        """Legacy ASCII VTK with POLYGONS / CELLS of tetrahedra
+        (lapy/_tet_io.py:131-224)."""
+        from ._meshio import read_vtk
+
+        v, t = read_vtk(filename, 4)
+        return cls(v, t)
+
+    def write_vtk(self, filename: str) -> None:
+        """Legacy ASCII VTK, in the reference's exact text
+        (lapy/_tet_io.py:227-259)."""
+        from ._meshio import write_vtk
+
+        write_vtk(self.v, self.t, filename)
+
     def avg_edge_length(self) -> float:
         """Mean edge length (lapy/tet_mesh.py:182-195), computed on the GPU."""
         from ._geometry import avg_edge_length

@@ -45,6 +45,33 @@ class TriaMesh:
     def is_2d(self) -> bool:
         return self._is_2d
 
+    # -- text file formats (lapy/_tria_io.py; host) -------------------------
+    @classmethod
+    def read_off(cls, filename: str) -> "TriaMesh":
+        """OFF file: optional ``#`` comment lines, ``OFF``, the counts, the
+        vertices (read as float32, as the reference does) and ``3 i j k``
+        faces (lapy/_tria_io.py:50-110)."""
+        from ._meshio import read_off
+
+        v, t = read_off(filename)
+        return cls(v, t)
+
+    @classmethod
+    def read_vtk(cls, filename: str) -> "TriaMesh":
+        """Legacy ASCII VTK with POLYGONS / CELLS of triangles or
+        TRIANGLE_STRIPS (lapy/_tria_io.py:113-227)."""
+        from ._meshio import read_vtk
+
+        v, t = read_vtk(filename, 3)
+        return cls(v, t)
+
+    def write_vtk(self, filename: str) -> None:
+        """Legacy ASCII VTK POLYDATA, in the reference's exact text
+        (lapy/_tria_io.py:638-674)."""
+        from ._meshio import write_vtk
+
+        write_vtk(self.v, self.t, filename)
+
     # -- host-side adjacency (mesh construction only) ---------------------
     def _adj_sym(self) -> sparse.csc_matrix:
         t0, t1, t2 = self.t[:, 0], self.t[:, 1], self.t[:, 2]
