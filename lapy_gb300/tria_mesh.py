@@ -4,8 +4,9 @@ Mirrors the constructor contract of lapy/tria_mesh.py:182-280 (TriaMesh):
 vertices ``v`` (n x 3, or n x 2 padded with z = 0), triangles ``t`` (m x 3),
 the same validation errors.  Geometry work that lies on the FEM path
 (``avg_edge_length``) runs on the GPU; ``refine_`` (host-side mesh
-construction) and the curvature pre-step of the anisotropic Laplacian live in
-NumPy, as inputs to the GPU kernels.
+construction), the measures used by spectra normalisation, the text file
+formats and the curvature pre-step of the anisotropic Laplacian
+(``curvature_tria``) live in NumPy, as inputs to the GPU kernels.
 """
 
 from __future__ import annotations
@@ -116,6 +117,59 @@ class TriaMesh:
     def area(self) -> float:
         """Total surface area (lapy/tria_mesh.py:660-669)."""
         return np.sum(self.tria_areas())
+
+    # -- curvature frame of the anisotropic Laplacian (host pre-step) -------
+    def tria_normals(self) -> np.ndarray:
+        """Unit triangle normals (lapy/tria_mesh.py:750-773)."""
+        from . import _curvature
+
+        return _curvature.tria_normals(self.v, self.t)
+
+    def vertex_normals(self) -> np.ndarray:
+        """Area-weighted vertex normals of an oriented mesh
+        (lapy/tria_mesh.py:775-817)."""
+        from . import _curvature
+
+        if not self.is_oriented():
+            raise ValueError("Error: Vertex normals are meaningless for un-oriented triangle meshes!")
+        return _curvature.vertex_normals(self.v, self.t)
+
+    def vertex_areas(self) -> np.ndarray:
+        """One third of the incident triangle areas (lapy/tria_mesh.py:715-733)."""
+        from . import _curvature
+
+        return _curvature.vertex_areas(self.v, self.t)
+
+    def smooth_laplace(self, vfunc=None, n: int = 1, lambda_: float = 0.5, mat=None) -> np.ndarray:
+        """Laplace smoothing of a vertex function (default: the vertices)
+        with the 1-ring averaging matrix (lapy/tria_mesh.py:1747-1792)."""
+        from . import _curvature
+
+        return _curvature.smooth_laplace(self.v, self.t, self.v if vfunc is None else vfunc, n, lambda_, mat)
+
+    def map_vfunc_to_tfunc(self, vfunc) -> np.ndarray:
+        """Triangle means of a vertex function (lapy/tria_mesh.py:1668-1694)."""
+        from . import _curvature
+
+        if self.v.shape[0] != np.asarray(vfunc).shape[0]:
+            raise ValueError("Error: length of vfunc needs to match number of vertices")
+        return _curvature.map_vfunc_to_tfunc(self.t, vfunc)
+
+    def curvature(self, smoothit: int = 3):
+        """Principal directions and curvatures at the vertices
+        (lapy/tria_mesh.py:1078-1219): u_min, u_max, c_min, c_max, c_mean,
+        c_gauss, normals."""
+        from . import _curvature
+
+        return _curvature.curvature(self.v, self.t, smoothit)
+
+    def curvature_tria(self, smoothit: int = 3):
+        """Principal directions and curvatures on the triangles, the frame of
+        the anisotropic Laplace-Beltrami assembly (lapy/tria_mesh.py:1221-1279):
+        u_min, u_max, c_min, c_max."""
+        from . import _curvature
+
+        return _curvature.curvature_tria(self.v, self.t, smoothit)
 
     def centroid(self) -> tuple[np.ndarray, float]:
         """Area-weighted mean of the triangle centres, and the total area
