@@ -42,6 +42,11 @@ const char* lapy_status_string(int status);
 const char* lapy_last_error(void);
 /* Kernel launches issued by this library since it was loaded. */
 long long lapy_launch_count(void);
+/* Diagnostics (host only): consistency of the persistent PCG's warp plan for
+ * the segments seg_row[0..nseg] (virtual warps / CTAs, reduction slots, row
+ * coverage).  LAPY_OK, or LAPY_ERR_INVALID with lapy_last_error() saying what
+ * failed. */
+int lapy_plan_check(const int32_t* seg_row, int nseg);
 /* PCG profile: when enabled, every persistent PCG launch is timed with CUDA
  * events and its work counted.  lapy_profile_read fills up to n of
  * {pcg_ms, pcg_launches, pcg_iterations, rows_processed, nnz_processed,

@@ -1443,3 +1443,58 @@ template int pcg_solve<double>(int64_t, const int32_t*, const int32_t*, const do
                                double*, double, int, int32_t*, void*, size_t, cudaStream_t, int*);
 
 }  // namespace lapy
+
+// Consistency of the persistent PCG's warp plan for the given segments (host
+// only, no device work): every virtual warp and virtual CTA holds at least one
+// piece, every reduction slot of a segment belongs to a virtual CTA that holds
+// a piece of it, pieces stay inside their segment, and the 32-row units of the
+// pieces cover every row exactly once.
+extern "C" int lapy_plan_check(const int32_t* seg_row, int nseg) {
+  using namespace lapy;
+  if (nseg < 0 || (nseg > 0 && !seg_row)) return LAPY_ERR_INVALID;
+  for (int s = 0; s < nseg; ++s)
+    if (seg_row[s + 1] < seg_row[s]) return LAPY_ERR_INVALID;
+  ChunkTable ct;
+  plan_chunks(seg_row, nseg, 4 * lapy_num_sms(), &ct);
+  auto fail = [](const char* what) {
+    lapy_set_last_message("plan_check: %s", what);
+    return LAPY_ERR_INVALID;
+  };
+  const int64_t total = nseg > 0 ? (int64_t)seg_row[nseg] - seg_row[0] : 0;
+  if (total > 0) {
+    for (int w = 0; w < ct.nvw; ++w)
+      if (ct.h_vw_piece[w + 1] <= ct.h_vw_piece[w]) return fail("a virtual warp holds no piece");
+    for (int v = 0; v < ct.nvc; ++v)
+      if (ct.h_vc_piece[v + 1] <= ct.h_vc_piece[v]) return fail("a virtual CTA holds no piece");
+  }
+  if (ct.nvc != (ct.nvw + kWarps - 1) / kWarps || ct.h_vc_piece[ct.nvc] != ct.npiece)
+    return fail("virtual CTA table");
+  std::vector<int> piece_vc(ct.npiece);
+  for (int w = 0; w < ct.nvw; ++w)
+    for (int32_t q = ct.h_vw_piece[w]; q < ct.h_vw_piece[w + 1]; ++q) piece_vc[q] = w / kWarps;
+  for (int s = 0; s < nseg; ++s) {
+    const int32_t q0 = ct.h_seg_piece[s], q1 = ct.h_seg_piece[s + 1];
+    const int ns = ct.h_seg_slot[s + 1] - ct.h_seg_slot[s];
+    if ((seg_row[s + 1] > seg_row[s]) != (q1 > q0)) return fail("segment without pieces");
+    if (q1 <= q0) {
+      if (ns != 0) return fail("slots of an empty segment");
+      continue;
+    }
+    std::vector<char> seen(ns, 0);
+    for (int32_t q = q0; q < q1; ++q) {
+      if (ct.h_piece_seg[q] != s) return fail("piece outside its segment");
+      const int k = piece_vc[q] - ct.h_seg_vc0[s];
+      if (k < 0 || k >= ns) return fail("piece outside its segment's slots");
+      seen[k] = 1;
+    }
+    for (int k = 0; k < ns; ++k)
+      if (!seen[k]) return fail("slot without a piece");
+  }
+  std::vector<int> cover(total, 0);
+  for (int q = 0; q < ct.npiece; ++q)
+    for (int32_t u = ct.h_piece_unit[q]; u < ct.h_piece_unit[q + 1]; ++u)
+      for (int32_t r = ct.h_unit_row[u]; r < ct.h_unit_row[u + 1]; ++r) cover[r - seg_row[0]]++;
+  for (int64_t r = 0; r < total; ++r)
+    if (cover[r] != 1) return fail("rows not covered exactly once");
+  return LAPY_OK;
+}

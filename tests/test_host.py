@@ -87,3 +87,28 @@ def test_sh_deformation_is_deterministic():
     assert np.array_equal(a.v, b.v)
     r = np.linalg.norm(a.v, axis=1)
     assert 0.5 < r.min() < r.max() < 1.5
+
+
+def test_pcg_warp_plan_is_consistent():
+    """The persistent PCG's warp plan (virtual warps and CTAs, per-CTA
+    reduction slots, row coverage) on random batches: tiny, empty and large
+    segments, and segment lengths that leave short tail units."""
+    from lapy_gb300 import _lib
+
+    L = _lib.lib()
+    rng = np.random.default_rng(7)
+    for trial in range(300):
+        nseg = int(rng.integers(1, 40))
+        if trial % 4 == 0:
+            lens = rng.integers(0, 40, nseg)
+        elif trial % 4 == 1:
+            lens = rng.integers(0, 3000, nseg)
+        else:
+            lens = rng.integers(1, 200, nseg) * 32 + rng.integers(0, 2, nseg) * rng.integers(1, 31, nseg)
+        if trial % 7 == 0:
+            lens[::3] = 0
+        seg_row = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+        st = L.lapy_plan_check(seg_row.ctypes.data, nseg)
+        assert st == 0, (trial, L.lapy_last_error().decode())
+    bad = np.array([0, 10, 5], dtype=np.int32)  # decreasing offsets are rejected
+    assert L.lapy_plan_check(bad.ctypes.data, 2) != 0
