@@ -20,6 +20,15 @@ class TetMesh:
             raise ValueError("Max index exceeds number of vertices")
 
     @classmethod
+    def read_gmsh(cls, filename: str) -> "TetMesh":
+        """ASCII gmsh 2.x file of tetrahedra (lapy/_tet_io.py:17-128); the
+        element node ids are taken as stored."""
+        from ._meshio import read_gmsh_tet
+
+        v, t = read_gmsh_tet(filename)
+        return cls(v, t)
+
+    @classmethod
     def read_vtk(cls, filename: str) -> "TetMesh":
         """Legacy ASCII VTK with POLYGONS / CELLS of tetrahedra
         (lapy/_tet_io.py:131-224)."""

@@ -73,6 +73,33 @@ class TriaMesh:
 
         write_vtk(self.v, self.t, filename)
 
+    @classmethod
+    def read_fssurf(cls, filename: str) -> "TriaMesh":
+        """FreeSurfer surface geometry with its volume-info footer in
+        ``fsinfo`` (lapy/_tria_io.py:16-47, lapy/_read_geometry.py:112-197)."""
+        from ._meshio import read_fssurf
+
+        v, t, info = read_fssurf(filename)
+        return cls(v, t, fsinfo=info)
+
+    def write_fssurf(self, filename: str, image=None, coords_are_voxels=None) -> None:
+        """FreeSurfer surface geometry, with ``fsinfo`` as the volume-info
+        footer (lapy/_tria_io.py:677-760).  Converting voxel coordinates with
+        an image header needs nibabel, as in the reference."""
+        from ._meshio import write_fssurf
+
+        if coords_are_voxels is None:
+            coords_are_voxels = image is not None
+        if coords_are_voxels and image is None:
+            raise ValueError(
+                "coords_are_voxels=True requires an image to be provided for voxel-to-surface-RAS "
+                "coordinate conversion. Either provide an image or set coords_are_voxels=False.")
+        if image is not None:
+            import nibabel  # noqa: F401  (image headers are nibabel objects)
+
+            raise NotImplementedError("image headers are not supported; pass coordinates in surface RAS")
+        write_fssurf(self.v, self.t, filename, volume_info=self.fsinfo)
+
     # -- host-side adjacency (mesh construction only) ---------------------
     def _adj_sym(self) -> sparse.csc_matrix:
         t0, t1, t2 = self.t[:, 0], self.t[:, 1], self.t[:, 2]

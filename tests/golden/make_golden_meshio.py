@@ -25,6 +25,8 @@ from make_golden import import_reference  # noqa: E402
 OFF_TEXT = "# a comment\nOFF\n4 2 0\n0 0 0\n1 0 0\n0 1 0\n1 1 0.5\n3 0 1 2\n3 1 3 2\n"
 VTK_CELLS = ("# vtk DataFile Version 2.0\nmesh\nASCII\nDATASET UNSTRUCTURED_GRID\nPOINTS 4 double\n"
              "0 0 0 1 0 0\n0 1 0 1 1 0.25\nCELLS 2 8\n3 0 1 2\n3 1 3 2\n")
+GMSH_TEXT = ("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n5\n1 0 0 0\n2 1 0 0\n3 0 1 0\n4 0 0 1\n"
+             "5 1 1 1\n$EndNodes\n$Elements\n2\n1 4 2 0 1 0 1 2 3\n2 4 2 0 1 1 2 3 4\n$EndElements\n")
 VTK_STRIPS = ("# vtk DataFile Version 1.0\nstrip\nASCII\nDATASET POLYDATA\nPOINTS 5 float\n"
               "0 0 0\n1 0 0\n0 1 0\n1 1 0\n0 2 0\nTRIANGLE_STRIPS 1 6\n5 0 1 2 3 4\n")
 
@@ -62,6 +64,27 @@ def main():
         out["write_kuhn5"] = np.array((tmp / "k.vtk").read_text())
         back = RTet.read_vtk(str(tmp / "k.vtk"))
         out["read_kuhn5_v"], out["read_kuhn5_t"] = back.v, back.t
+        # gmsh tetrahedra (ASCII 2.2; element rows: id, type 4, 2 tags, 4 node ids)
+        (tmp / "k.msh").write_text(GMSH_TEXT)
+        m = RTet.read_gmsh(str(tmp / "k.msh"))
+        out["gmsh_text"], out["gmsh_v"], out["gmsh_t"] = np.array(GMSH_TEXT), m.v, m.t
+        # FreeSurfer surfaces written by lapy_gb300's writer, read by the reference
+        sys.path.insert(0, str(HERE.parent.parent))
+        from lapy_gb300._meshio import write_fssurf
+
+        f = np.load(HERE / "ref_deformed3.npz")
+        info = {"head": [2, 0, 20], "valid": "1  # volume info valid", "filename": "vol.mgz",
+                "volume": np.array([256, 256, 256]), "voxelsize": np.array([1.0, 1.0, 1.0]),
+                "xras": np.array([-1.0, 0.0, 0.0]), "yras": np.array([0.0, 0.0, -1.0]),
+                "zras": np.array([0.0, 1.0, 0.0]), "cras": np.array([0.5, -12.25, 3.0])}
+        for tag, vi in (("plain", None), ("volinfo", info)):
+            write_fssurf(f["v"], f["t"], str(tmp / "s.surf"), volume_info=vi)
+            out[f"fs_{tag}_bytes"] = np.frombuffer((tmp / "s.surf").read_bytes(), dtype=np.uint8)
+            m = RTria.read_fssurf(str(tmp / "s.surf"))
+            out[f"fs_{tag}_v"], out[f"fs_{tag}_t"] = m.v, m.t
+            if vi is not None:
+                for key, val in m.fsinfo.items():
+                    out[f"fs_{tag}_info_{key}"] = np.asarray(val)
     np.savez_compressed(HERE / "ref_meshio.npz", **out)
     print("wrote", HERE / "ref_meshio.npz", sorted(out))
 

@@ -1,6 +1,7 @@
-"""OFF / legacy VTK mesh files against the reference's own readers and
-writers (tests/golden/ref_meshio.npz, made by make_golden_meshio.py).  Host
-code only."""
+"""Mesh files against the reference's own readers and writers
+(tests/golden/ref_meshio.npz, made by make_golden_meshio.py): OFF, legacy
+ASCII VTK, ASCII gmsh tetrahedra and FreeSurfer surface geometry.  Host code
+only."""
 
 from __future__ import annotations
 
@@ -94,3 +95,47 @@ def test_reader_errors(ref, tmp_path):
     tria_text = str(ref["write_ico3_float64"])
     with pytest.raises(ValueError, match="data per tetra"):  # and the other way round (ValueError, as the reference)
         TetMesh.read_vtk(_write(tmp_path, "r.vtk", tria_text))
+
+
+def test_gmsh_tetrahedra(ref, tmp_path):
+    from lapy_gb300 import TetMesh
+
+    m = TetMesh.read_gmsh(_write(tmp_path, "k.msh", ref["gmsh_text"]))
+    np.testing.assert_array_equal(m.v, ref["gmsh_v"])
+    assert m.v.dtype == ref["gmsh_v"].dtype
+    np.testing.assert_array_equal(m.t, ref["gmsh_t"])
+    with pytest.raises(ValueError, match="no .msh file"):
+        TetMesh.read_gmsh(_write(tmp_path, "k.txt", ref["gmsh_text"]))
+    with pytest.raises(ValueError, match="binary format"):
+        TetMesh.read_gmsh(_write(tmp_path, "b.msh", str(ref["gmsh_text"]).replace("2.2 0 8", "2.2 1 8")))
+    with pytest.raises(ValueError, match="can only read tetras"):
+        TetMesh.read_gmsh(_write(tmp_path, "c.msh", str(ref["gmsh_text"]).replace("1 4 2 0 1", "1 2 2 0 1")))
+
+
+@pytest.mark.parametrize("tag", ["plain", "volinfo"])
+def test_freesurfer_surface(ref, tmp_path, tag):
+    """Files written here are read by the reference's FreeSurfer reader (the
+    fixture holds what it returned) and by this reader alike."""
+    from lapy_gb300 import TriaMesh
+
+    f = np.load(GOLD / "ref_deformed3.npz")
+    info = None
+    if tag == "volinfo":
+        info = {k: ref[f"fs_volinfo_info_{k}"] for k in ("head", "valid", "filename", "volume", "voxelsize",
+                                                          "xras", "yras", "zras", "cras")}
+        info = {k: (str(v) if v.dtype.kind == "U" else v) for k, v in info.items()}
+    p = str(tmp_path / "s.surf")
+    TriaMesh(f["v"], f["t"], fsinfo=info).write_fssurf(p)
+    assert np.array_equal(np.frombuffer(Path(p).read_bytes(), dtype=np.uint8), ref[f"fs_{tag}_bytes"])
+    m = TriaMesh.read_fssurf(p)
+    np.testing.assert_array_equal(m.v, ref[f"fs_{tag}_v"])
+    np.testing.assert_array_equal(m.t, ref[f"fs_{tag}_t"])
+    if tag == "volinfo":
+        for key, val in m.fsinfo.items():
+            np.testing.assert_array_equal(np.asarray(val), ref[f"fs_volinfo_info_{key}"])
+    else:
+        assert len(m.fsinfo) == 0
+    bad = tmp_path / "bad.surf"
+    bad.write_bytes(b"\x00\x01\x02rest")
+    with pytest.raises(ValueError, match="Freesurfer"):
+        TriaMesh.read_fssurf(str(bad))
