@@ -54,3 +54,28 @@ def test_single_rank_time_is_local():
 
     assert bench.max_over_ranks(3.25, 1) == 3.25
     assert bench.rank_seed(5, 0) == 5 and bench.rank_seed(5, 1) != 5
+
+
+def test_reference_arm_json_contract():
+    """`bench.py --impl reference` (the SciPy method on the host cores) prints
+    one JSON line with the keys the measurement contract needs."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    out = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--meshes", "8",
+                          "--cpu-per-level", "1", "--steps", "1", "--warmup", "0"],
+                         capture_output=True, text=True, timeout=600, cwd=str(root))
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "spectra/s"
+    assert line["e2e"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert "workload" in line["config"]
