@@ -47,3 +47,28 @@ def test_status_strings_without_gpu():
     assert L.lapy_fem_numeric_workspace_bytes(100, 3) > 100 * 9 * 8 * 2
     assert L.lapy_csr_symbolic_workspace_bytes(50, 100, 4) > 0
     assert L.lapy_csr_symbolic_workspace_bytes(50, 100, 5) == 0
+
+
+def test_argument_checks_before_any_device_work():
+    """Entry points reject bad sizes before touching the device (no GPU
+    needed): the heat-kernel product and the plan check."""
+    import ctypes as C
+
+    import numpy as np
+
+    from lapy_gb300 import _lib
+
+    L = _lib.lib()
+    fake = C.c_void_p(16)  # never dereferenced: the checks fail first
+    # ld < nev
+    assert L.lapy_heat_product_f64(4, None, fake, 2, 3, 0, fake, 1, fake, None) == _lib.ERR_INVALID
+    # negative sizes
+    assert L.lapy_heat_product_f64(-1, None, fake, 3, 3, 0, fake, 1, fake, None) == _lib.ERR_INVALID
+    assert L.lapy_heat_product_f64(4, None, fake, 3, 3, 0, fake, -2, fake, None) == _lib.ERR_INVALID
+    # empty output: nothing to do
+    assert L.lapy_heat_product_f64(0, None, fake, 3, 3, 0, fake, 1, fake, None) == 0
+    # null data pointers
+    assert L.lapy_heat_product_f64(4, None, None, 3, 3, 0, fake, 1, fake, None) == _lib.ERR_INVALID
+    seg = np.array([0, 5], dtype=np.int32)
+    assert L.lapy_plan_check(seg.ctypes.data, -1) == _lib.ERR_INVALID
+    assert L.lapy_plan_check(seg.ctypes.data, 1) == 0
