@@ -134,7 +134,36 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- CPU baseline
+def workload_name(n_meshes: int, n_vertices: int) -> str:
+    """The batched workload's name; both arms print the same string."""
+    return (f"batched ShapeDNA: {n_meshes} deformed icospheres (levels 3-6, {n_vertices} vertices), k=50, "
+            f"sigma=-0.01, consistent mass")
+
+
+def cpu_model() -> str:
+    """Host CPU model (lscpu's 'Model name', else /proc/cpuinfo, else the machine)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
 def _cpu_one(args):
+    """One mesh through the reference method: assembly + eigsh/splu (k
+    eigenpairs), then the splu heat step.  Returns the two times and both
+    results (eigenvalues, heat solution) for the accuracy check."""
     v, t, k = args
     import oracle
 
@@ -142,27 +171,24 @@ def _cpu_one(args):
     A, M = oracle.assemble_scipy(v, t)
     ev, _ = oracle.eigs(A, M, k=k)
     t1 = time.perf_counter()
-    oracle.diffusion(v, t, 0, m=1.0)
-    return t1 - t0, time.perf_counter() - t1
+    u = oracle.diffusion(v, t, 0, m=1.0)
+    return t1 - t0, time.perf_counter() - t1, np.sort(ev), u
 
 
-def cpu_baseline(meshes, lv, per_level: int = 4, cores: int | None = None):
-    """Reference CPU method (assembly + splu/eigsh; splu heat step) on a
-    stratified sample, all cores.  Returns (spectra baseline, heat baseline)."""
+def _run_pool(work, cores, fn=_cpu_one):
+    """Run `fn` over `work` in a spawn pool, one item per worker at a time,
+    BLAS threads 1; returns (results, wall seconds of the timed map)."""
     import multiprocessing as mp
 
-    cores = cores or len(os.sched_getaffinity(0))
-    idx = stratified(lv, per_level)
-    work = [(meshes[i].v, meshes[i].t, K_EIG) for i in idx]
     env = {"OPENBLAS_NUM_THREADS": "1", "OMP_NUM_THREADS": "1", "MKL_NUM_THREADS": "1"}
     old = {k: os.environ.get(k) for k in env}
     os.environ.update(env)
     try:
         ctx = mp.get_context("spawn")
         with ctx.Pool(processes=min(cores, len(work))) as pool:
-            pool.map(_cpu_one, work[:1])  # warm the workers' imports
+            pool.map(fn, work[:1])  # warm the workers' imports
             t0 = time.perf_counter()
-            secs = pool.map(_cpu_one, work, chunksize=1)
+            res = pool.map(fn, work, chunksize=1)
             wall = time.perf_counter() - t0
     finally:
         for k, v in old.items():
@@ -170,19 +196,63 @@ def cpu_baseline(meshes, lv, per_level: int = 4, cores: int | None = None):
                 os.environ.pop(k, None)
             else:
                 os.environ[k] = v
+    return res, wall
+
+
+def cpu_baseline(meshes, lv, per_level: int = 4, cores: int | None = None):
+    """Reference CPU method (assembly + splu/eigsh; splu heat step) on a
+    stratified sample, all cores.  Returns (spectra baseline, heat baseline,
+    sample results {idx, ev, u, wall})."""
+    cores = cores or len(os.sched_getaffinity(0))
+    idx = stratified(lv, per_level)
+    work = [(meshes[i].v, meshes[i].t, K_EIG) for i in idx]
+    res, wall = _run_pool(work, cores)
     # Throughput on the whole batch: mean CPU seconds per mesh of each level
     # (measured on the sample, one mesh per worker process) times the batch's
     # level counts, spread over all cores.
-    total, by_level = extrapolate(lv, idx, [e for e, _ in secs])
-    total_h, by_level_h = extrapolate(lv, idx, [h for _, h in secs])
+    total, by_level = extrapolate(lv, idx, [r[0] for r in res])
+    total_h, by_level_h = extrapolate(lv, idx, [r[1] for r in res])
+    model = cpu_model()
     sample = (f"{len(work)} meshes ({per_level} per icosphere level 3-6) timed one per worker "
               f"(BLAS threads 1, sample wall {wall:.1f} s); the batch's CPU seconds "
               f"({{:.0f}}) spread over {cores} cores")
     spectra = {"value": len(meshes) / (total / cores), "unit": "spectra/s", "cores": cores, "kind": "port",
-               "sample": sample.format(total), "sec_per_mesh_by_level": by_level}
+               "cpu_model": model, "sample": sample.format(total), "sec_per_mesh_by_level": by_level,
+               "sample_wall_s": wall}
     heat = {"value": len(meshes) / (total_h / cores), "unit": "heat solves/s", "cores": cores, "kind": "port",
-            "sample": sample.format(total_h) + " (splu of M + t A, lumped M)", "sec_per_mesh_by_level": by_level_h}
-    return spectra, heat
+            "cpu_model": model, "sample": sample.format(total_h) + " (splu of M + t A, lumped M)",
+            "sec_per_mesh_by_level": by_level_h}
+    return spectra, heat, {"idx": idx, "ev": [r[2] for r in res], "u": [r[3] for r in res], "wall": wall}
+
+
+def eig_accuracy(gpu_ev: np.ndarray, idx, ref_evs) -> dict:
+    """GPU eigenvalues of meshes `idx` against the reference call's (eigsh in
+    shift-invert mode with splu, lapy/solver.py:702-716): the largest relative
+    error of lambda_1..lambda_{k-1}, and |lambda_0 - ref| / lambda_1 (lambda_0 ~ 0)."""
+    rel, l0 = [], []
+    for i, ref in zip(idx, ref_evs):
+        g = np.asarray(gpu_ev[i], dtype=np.float64)
+        lam1 = abs(ref[1])
+        l0.append(abs(g[0] - ref[0]) / lam1)
+        rel.append(float(np.max(np.abs(g[1:] - ref[1:]) / np.abs(ref[1:]))))
+    return {"max_eig_rel_err": max(rel), "lambda0_abs_over_lambda1": max(l0), "meshes_checked": len(idx),
+            "against": "scipy eigsh shift-invert + splu (the reference's call) on the host"}
+
+
+def heat_accuracy(meshes, x_dev, seg_row, idx, ref_us) -> dict:
+    """Batched GPU heat solutions against the reference's splu solve, in the
+    lumped-mass norm: max_s ||u - u_ref||_M / ||u_ref||_M."""
+    import oracle
+
+    x = x_dev.cpu().numpy()
+    errs = []
+    for i, ref in zip(idx, ref_us):
+        _, M = oracle.assemble_scipy(meshes[i].v, meshes[i].t, lump=True)
+        w = M.diagonal()
+        u = x[seg_row[i]:seg_row[i + 1]]
+        errs.append(float(np.sqrt(np.sum(w * (u - ref) ** 2) / np.sum(w * ref ** 2))))
+    return {"max_mnorm_rel_err": max(errs), "meshes_checked": len(idx),
+            "against": "scipy splu of M + t A (the reference's call) on the host"}
 
 
 # ----------------------------------------------------------------------------- GPU arm
@@ -238,9 +308,9 @@ def run_gpu(args, rank, world):
     t_max = max_over_ranks(dev_s, world)
     status_ok = all(int(s) == 0 for inf in infos for s in inf["status"])
 
-    # e2e through the public API from host buffers
+    # e2e through the public API from host buffers (mean over e2e_steps calls)
     torch.cuda.synchronize()
-    e2e_steps = 0 if args.no_e2e else 1
+    e2e_steps = 0 if args.no_e2e else args.e2e_steps
     te = time.perf_counter()
     for _ in range(e2e_steps):
         res = shapedna.compute_shapedna_batch(meshes, k=K_EIG, block=args.block, return_vectors=False)
@@ -257,13 +327,12 @@ def run_gpu(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 inner PCG / f64 Lanczos, Ritz and refinement", "data": "synthetic",
-        "config": {"workload": f"batched ShapeDNA: {args.meshes} deformed icospheres (levels 3-6, "
-                               f"{n_total} vertices), k=50, sigma=-0.01, consistent mass",
+        "config": {"workload": workload_name(args.meshes, n_total),
                    "block": args.block, "per_gpu_meshes": args.meshes,
                    "l2": "inputs larger than L2 (batch CSR + Krylov basis >> 129 MB)",
                    "parallelism": f"replicas x{world} (meshes sharded, no collective)"},
         "e2e": ({"value": world * args.meshes * e2e_steps / te, "unit": "spectra/s", "h2d_bytes_per_step": h2d,
-                 "d2h_bytes_per_step": d2h} if e2e_steps else None),
+                 "d2h_bytes_per_step": d2h, "calls": e2e_steps} if e2e_steps else None),
         "roofline": {"bound": "hbm", "kernel": "pcg_kernel (persistent FP32 Jacobi-PCG)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": None,
@@ -272,20 +341,25 @@ def run_gpu(args, rank, world):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "status_ok": status_ok,
-        "pcg": {k: prof[k] for k in ("pcg_launches", "pcg_iterations", "rows", "nnz")},
+        "pcg": {**{k: prof[k] for k in ("pcg_launches", "pcg_iterations", "rows", "nnz")},
+                "phase_ms": {k[6:-3]: prof[k] for k in prof if k.startswith("phase_")}},
         "lanczos": {"segment_steps": prof["lanczos_segment_steps"], "second_cgs_passes": prof["second_cgs_passes"]},
         "wall_s": wall,
     }
+    heat_x = None
     if not args.no_heat:
-        line["heat"] = run_heat(args, meshes, lv, batch_in, world)
+        line["heat"], heat_x = run_heat(args, meshes, lv, batch_in, world)
     if not args.no_plain:
         line["plain"] = run_plain_spectra(args, meshes, lv, line["value"] / world)
     if not args.no_learned:
         line["learned"] = run_learned(args)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"], heat_cpu = cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
+        line["cpu_baseline"], heat_cpu, ref = cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
+        # accuracy of the timed step's eigenvalues on the CPU arm's sample
+        line["accuracy"] = eig_accuracy(evals.cpu().numpy(), ref["idx"], ref["ev"])
         if "heat" in line:
             line["heat"]["cpu_baseline"] = heat_cpu
+            line["heat"]["accuracy"] = heat_accuracy(meshes, heat_x, batch_in.seg_row, ref["idx"], ref["u"])
     return line
 
 
@@ -317,13 +391,16 @@ def run_heat(args, meshes, lv, batch_in, world):
     def step():
         x, info = hb.solve()
         out["info"] = info
+        out["x"] = x
 
     dev_s = max_over_ranks(_timed(step, args.steps, args.warmup), world)
     relres = float(np.max(out["info"]["relres"]))
+    e2e_calls = 0 if args.no_e2e else args.e2e_steps
+    torch.cuda.synchronize()
     te = time.perf_counter()
-    if not args.no_e2e:
+    for _ in range(e2e_calls):
         heat.diffusion_batch(meshes, 0, m=1.0)
-        torch.cuda.synchronize()
+    torch.cuda.synchronize()
     te = time.perf_counter() - te
     # plain: the unbatched API, one mesh at a time
     idx = stratified(lv, args.plain_per_level)
@@ -340,13 +417,14 @@ def run_heat(args, meshes, lv, batch_in, world):
     plain = args.meshes / total
     return {"value": value, "unit": "heat solves/s", "ms_per_step": dev_s * 1e3 / args.steps,
             "max_relres": relres, "pcg_iterations": int(out["info"]["iters"]),
-            "e2e": ({"value": world * args.meshes / te, "unit": "heat solves/s",
+            "e2e": ({"value": world * args.meshes * e2e_calls / te, "unit": "heat solves/s",
                      "h2d_bytes_per_step": sum(m.v.nbytes + m.t.size * 4 for m in meshes) + 8 * len(meshes),
-                     "d2h_bytes_per_step": 8 * sum(len(m.v) for m in meshes)} if not args.no_e2e else None),
+                     "d2h_bytes_per_step": 8 * sum(len(m.v) for m in meshes), "calls": e2e_calls}
+                    if e2e_calls else None),
             "plain": {"value": world * plain, "unit": "heat solves/s",
                       "sample": f"{len(idx)} meshes ({args.plain_per_level} per level) through heat.diffusion one "
                                 f"at a time, extrapolated by level counts", "sec_per_mesh_by_level": by_level},
-            "vs_plain": value / (world * plain)}
+            "vs_plain": value / (world * plain)}, out["x"]
 
 
 def run_learned(args):
@@ -394,37 +472,86 @@ def _single_mesh(args):
     return meshes.deformed_icospheres([8], [args.seed])[0]
 
 
-def _c2_heat_steps(fem, mesh, steps=10, t=1e-3):
-    """u_{k+1} = (M + t A)^-1 M u_k from the centre vertex (consistent M)."""
+def _c2_heat_steps(fem, mesh, steps=10, t=1e-3, residuals=False):
+    """u_{k+1} = (M + t A)^-1 M u_k from the centre vertex (consistent M).
+    With ``residuals``, also the FP64 true residual of every step,
+    ||M u_k - (M + t A) u_{k+1}|| / ||M u_k|| (computed on the device)."""
     import torch
 
     from lapy_gb300 import meshes
-    from lapy_gb300._device import axpby, pcg_solve
+    from lapy_gb300._device import DeviceCSR, axpby, pcg_solve
 
     A = fem._A.as_f64()
     M = fem._M.as_f64()
     kv = M.on_pattern(A.indptr, A.indices, A.data.numel())
     axpby(t, A.data.contiguous(), 1.0, kv, out=kv)
+    K = DeviceCSR(A.n, A.indptr, A.indices, kv)
     u = torch.zeros(A.n, dtype=torch.float64, device="cuda")
     u[meshes.kuhn_center_vertex(64)] = 1.0
+    res = []
     for _ in range(steps):
-        u, _, _ = pcg_solve(A.indptr, A.indices, kv, A.n, kv.numel(), M.matmul(u), 1e-10)
-    return u
+        b = M.matmul(u)
+        u, _, _ = pcg_solve(A.indptr, A.indices, kv, A.n, kv.numel(), b, 1e-10)
+        if residuals:
+            res.append(float(torch.linalg.norm(b - K.matmul(u)) / torch.linalg.norm(b)))
+    return (u, res) if residuals else u
+
+
+def eig_certificate(fem, ev: np.ndarray, X: np.ndarray) -> dict:
+    """FP64 certificate of computed eigenpairs, on the device: the largest
+    relative Ritz residual ||A x - lam M x|| / (max(|lam|, lam_1) ||M x||) and
+    the largest entry of X'MX - I (M-orthonormality)."""
+    import torch
+
+    A = fem._A.as_f64()
+    M = fem._M.as_f64()
+    Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64)).to("cuda")
+    lam = torch.from_numpy(np.asarray(ev, dtype=np.float64)).to("cuda")
+    AX, MX = A.matmul(Xd), M.matmul(Xd)
+    R = AX - MX * lam[None, :]
+    scale = torch.clamp(lam.abs(), min=abs(float(ev[1])))
+    rel = torch.linalg.norm(R, dim=0) / (scale * torch.linalg.norm(MX, dim=0))
+    G = Xd.T @ MX
+    orth = (G - torch.eye(G.shape[0], dtype=G.dtype, device=G.device)).abs().max()
+    return {"max_ritz_residual": float(rel.max()), "max_orthonormality_err": float(orth), "pairs": int(len(ev))}
+
+
+def heat_certificate(mesh, u: np.ndarray, vid: int = 0, m: float = 1.0) -> dict:
+    """FP64 true residual of a heat step (M + t A) u = e_vid with lumped M and
+    t = m * mean edge length^2 (lapy/heat.py:204-227), on the device."""
+    import torch
+
+    from lapy_gb300 import Solver
+    from lapy_gb300._device import DeviceCSR, axpby
+
+    fem = Solver(mesh, lump=True)
+    t = m * mesh.avg_edge_length() ** 2
+    A = fem._A.as_f64()
+    hv = fem._M.as_f64().on_pattern(A.indptr, A.indices, A.data.numel())
+    axpby(t, A.data.contiguous(), 1.0, hv, out=hv)
+    K = DeviceCSR(A.n, A.indptr, A.indices, hv)
+    ud = torch.from_numpy(np.ascontiguousarray(u, dtype=np.float64)).to("cuda")
+    b = torch.zeros_like(ud)
+    b[vid] = 1.0
+    return {"heat_true_relres": float(torch.linalg.norm(b - K.matmul(ud)) / torch.linalg.norm(b))}
 
 
 def _cpu_single(workload, v, t, seed):
-    """The reference method on one host core (oracle: SciPy splu + eigsh)."""
+    """The reference method on one host core (oracle: SciPy splu + eigsh).
+    Returns (seconds, results for the accuracy check)."""
     import oracle
 
+    out = {}
     t0 = time.perf_counter()
     if workload == "sphere-l5":
         A, M = oracle.assemble_scipy(v, t)
-        oracle.eigs(A, M, k=50)
+        ev, _ = oracle.eigs(A, M, k=50)
+        out["ev"] = np.sort(ev)
     elif workload == "kuhn-64":
         from scipy.sparse.linalg import splu
 
         A, M = oracle.assemble_scipy(v, t)
-        oracle.eigs(A, M, k=100)
+        out["ev"] = np.sort(oracle.eigs(A, M, k=100)[0])
         lu = splu((M + 1e-3 * A).tocsc())
         u = np.zeros(len(v))
         n = round(len(v) ** (1 / 3)) - 1
@@ -433,8 +560,9 @@ def _cpu_single(workload, v, t, seed):
             u = lu.solve(M @ u)
     else:
         u = oracle.diffusion(v, t, 0, m=1.0)
-        oracle.geodesic_f(v, t, u)
-    return time.perf_counter() - t0
+        out["u"] = u
+        out["d"] = oracle.geodesic_f(v, t, u)
+    return time.perf_counter() - t0, out
 
 
 def cpu_single(workload, mesh, seed, timeout):
@@ -445,20 +573,23 @@ def cpu_single(workload, mesh, seed, timeout):
     with ctx.Pool(1) as pool:
         res = pool.apply_async(_cpu_single, (workload, np.asarray(mesh.v), np.asarray(mesh.t), seed))
         try:
-            secs = res.get(timeout=timeout)
+            secs, out = res.get(timeout=timeout)
         except mp.TimeoutError:
             pool.terminate()
-            return {"value": None, "unit": "runs/s", "cores": 1, "kind": "port",
-                    "sample": f"one run of the reference method did not finish within {timeout:.0f} s"}
+            return {"value": None, "unit": "runs/s", "cores": 1, "kind": "port", "cpu_model": cpu_model(),
+                    "sample": f"one run of the reference method did not finish within {timeout:.0f} s"}, None
     return {"value": 1.0 / secs, "unit": "runs/s", "cores": 1, "kind": "port", "seconds": secs,
-            "sample": "one full run of the reference method (SciPy splu + eigsh / splu solves), one core"}
+            "cpu_model": cpu_model(),
+            "sample": "one full run of the reference method (SciPy splu + eigsh / splu solves), one core"}, out
 
 
 def run_single(args):
     """sphere-l5 (icosphere L5, eigs 50), kuhn-64 (Kuhn 64^3 tets: eigs 100 + 10
     heat steps), sphere-l8-geodesics (deformed icosphere L8: heat + heat-method
     geodesics), from host arrays
-    through the public API each step (so value and e2e coincide)."""
+    through the public API each step (so value and e2e coincide).  After the
+    timed steps the last step's results get an FP64 certificate computed on
+    the device and, where the CPU run finishes, a comparison with it."""
     import torch
 
     from lapy_gb300 import Solver, TetMesh, TriaMesh, diffgeo, heat
@@ -470,18 +601,19 @@ def run_single(args):
     def step():
         mesh = cls(mesh0.v.copy(), mesh0.t.copy())  # fresh upload every step
         if args.workload == "sphere-l5":
-            ev, _ = Solver(mesh, lump=False).eigs(k=50)
-            info["ev"] = ev
+            fem = Solver(mesh, lump=False)
+            info["ev"], info["X"] = fem.eigs(k=50)
+            info["fem"] = fem
         elif args.workload == "kuhn-64":
             fem = Solver(mesh, lump=False)
-            ev, _ = fem.eigs(k=100)
+            info["ev"], info["X"] = fem.eigs(k=100)
             u = _c2_heat_steps(fem, mesh)
-            info["ev"] = ev
+            info["fem"] = fem
             info["u_sum"] = float(u.sum())
         else:
             u = heat.diffusion(mesh, 0, m=1.0)
             d = diffgeo.compute_geodesic_f(mesh, u)
-            info["dmax"] = float(np.max(d))
+            info["u"], info["d"] = u, d
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
@@ -496,39 +628,72 @@ def run_single(args):
              "sphere-l8-geodesics": ("runs/s (deformed icosphere L8: heat + geodesics)", "runs/s")}
     metric, unit = names[args.workload]
     v = args.steps / wall
+    # FP64 certificates of the last step's results (outside the timed region)
+    cert = {}
+    if "ev" in info:
+        cert.update(eig_certificate(info["fem"], info["ev"], info["X"]))
+    if args.workload == "kuhn-64":
+        _, res = _c2_heat_steps(info["fem"], None, residuals=True)
+        cert["heat_max_true_relres"] = max(res)
+        cert["heat_steps"] = len(res)
+    if args.workload == "sphere-l8-geodesics":
+        cert.update(heat_certificate(mesh0, info["u"]))
     line = {"metric": metric, "value": v, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 inner PCG / f64 Lanczos and refinement", "data": "synthetic",
             "config": {"workload": args.workload, "vertices": int(len(mesh0.v)), "elements": int(len(mesh0.t))},
             "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": int(mesh0.v.nbytes + mesh0.t.size * 4),
                     "d2h_bytes_per_step": int(8 * (50 if args.workload == "sphere-l5" else len(mesh0.v)))},
-            "clocks": clk.summary(), "check": {k: (float(np.asarray(x).ravel()[-1]) if k == "ev" else x)
-                                               for k, x in info.items()}}
+            "clocks": clk.summary(), "certificate": cert}
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_single(args.workload, mesh0, args.seed, args.cpu_timeout)
+        line["cpu_baseline"], ref = cpu_single(args.workload, mesh0, args.seed, args.cpu_timeout)
+        acc = {}
+        if ref is not None and "ev" in ref and "ev" in info:
+            acc = eig_accuracy(np.asarray(info["ev"])[None, :], [0], [ref["ev"]])
+        if ref is not None and "u" in ref:
+            import oracle
+
+            _, Ml = oracle.assemble_scipy(mesh0.v, mesh0.t, lump=True)
+            w = Ml.diagonal()
+            acc["heat_mnorm_rel_err"] = float(np.sqrt(np.sum(w * (info["u"] - ref["u"]) ** 2) /
+                                                      np.sum(w * ref["u"] ** 2)))
+            acc["geodesic_max_abs_diff_over_max"] = float(np.max(np.abs(info["d"] - ref["d"])) /
+                                                          np.max(np.abs(ref["d"])))
+            acc["against"] = "the reference method on the host (splu heat step; geodesics with its singular splu)"
+        if acc:
+            line["accuracy"] = acc
     return line
 
 
 def run_reference(args):
+    """The reference's CPU method (the oracle's restatement: SciPy splu +
+    eigsh, splu heat step) on the host cores.  One step = one stratified
+    sample of the batch (per_level meshes of each level), timed; the batch's
+    throughput is extrapolated from the per-level CPU seconds."""
     meshes, lv = make_batch(args.meshes, seed=args.seed)
-    vals = []
+    n_total = sum(len(m.v) for m in meshes)
     for _ in range(args.warmup):
-        pass  # the CPU method has no warm-up state beyond imports (done in the pool)
-    heats = []
+        cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
+    vals, heats, walls = [], [], []
     for _ in range(args.steps):
-        sp, ht = cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
+        t0 = time.perf_counter()
+        sp, ht, _ = cpu_baseline(meshes, lv, per_level=args.cpu_per_level)
+        walls.append(time.perf_counter() - t0)
         vals.append(sp)
         heats.append(ht)
     v = statistics.median([x["value"] for x in vals])
     base = vals[0]
     hv = statistics.median([x["value"] for x in heats])
     return {"metric": METRIC, "value": v, "unit": "spectra/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * (args.cpu_per_level * 4) / v, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(walls), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"batched ShapeDNA: {args.meshes} deformed icospheres (levels 3-6), k=50"},
+            "config": {"workload": workload_name(args.meshes, n_total),
+                       "step": f"one stratified sample of {args.cpu_per_level * 4} meshes ({args.cpu_per_level} per "
+                               f"level) through the CPU method, wall-timed; value extrapolates the per-level CPU "
+                               f"seconds to the {args.meshes}-mesh batch over {base['cores']} cores"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "spectra/s", "cores": base["cores"], "kind": "port",
-                             "sample": base["sample"]},
+                             "cpu_model": base["cpu_model"], "sample": base["sample"]},
             "e2e": {"value": v, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "heat": {"value": hv, "unit": "heat solves/s", "cpu_baseline": heats[0]}}
 
@@ -553,6 +718,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-test", type=int, default=32, help="held-out level-7 meshes of the learned-SPAI leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the public-API end-to-end leg (profiling runs)")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="public-API calls averaged by the e2e legs")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -50,7 +50,11 @@ int lapy_plan_check(const int32_t* seg_row, int nseg);
 /* PCG profile: when enabled, every persistent PCG launch is timed with CUDA
  * events and its work counted.  lapy_profile_read fills up to n of
  * {pcg_ms, pcg_launches, pcg_iterations, rows_processed, nnz_processed,
- *  algorithmic_bytes, lanczos_segment_steps, second_cgs_passes}. */
+ *  algorithmic_bytes, lanczos_segment_steps, second_cgs_passes,
+ *  then 7 per-phase milliseconds of the PCG launches (device clock between
+ *  grid barriers): initialisation, SpMM, update, coarse restriction, coarse
+ *  solve, direction update, final publication}. */
+#define LAPY_PCG_PHASES 7
 void lapy_profile_enable(int on);
 void lapy_profile_reset(void);
 int lapy_profile_read(double* out, int n);
@@ -115,6 +119,18 @@ int lapy_fem_tet_numeric(const void* v, int coords_f32, const int32_t* t, int64_
                          const int32_t* seg_ptr, const int32_t* seg_src, int64_t nnz,
                          int lump, int out_f32, void* a_vals, void* m_vals, void* work,
                          size_t ws_bytes, void* stream);
+/* Batched form of lapy_fem_tria_numeric (npe 3) / lapy_fem_tet_numeric
+ * (npe 4) for meshes concatenated into one block-diagonal system: seg_elem
+ * (device, nseg+1 int32, nondecreasing from 0 to m) gives each mesh's element
+ * range, and each mesh's degenerate elements are clamped with that mesh's own
+ * mean measure, as one lapy/solver.py:158-159 (:436-437) call per mesh does.
+ * `work` must hold lapy_fem_batch_numeric_workspace_bytes(m, npe, nseg). */
+size_t lapy_fem_batch_numeric_workspace_bytes(int64_t m, int npe, int nseg);
+int lapy_fem_batch_numeric(int npe, const void* v, int coords_f32, const int32_t* t, int64_t m,
+                           int nseg, const int32_t* seg_elem, int64_t n, const int32_t* indptr,
+                           const int32_t* indices, const int32_t* seg_ptr, const int32_t* seg_src,
+                           int64_t nnz, int lump, int out_f32, void* a_vals, void* m_vals, void* work,
+                           size_t ws_bytes, void* stream);
 
 /* Position of the diagonal entry of every row (-1 if absent). */
 int lapy_csr_diag_index(int64_t n, const int32_t* indptr, const int32_t* indices,
@@ -213,8 +229,12 @@ int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices,
  * GPU loading the library holds until exit.  Problems needing more scratch
  * (lapy_pcg_solve_workspace_bytes) are rejected with LAPY_ERR_WORKSPACE.  The
  * first call on a device looks up the array's address (cudaGetSymbolAddress)
- * and should come before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race.  Nothing is allocated or freed. */
+ * and should come before any stream capture; the address is kept for the
+ * life of the process, so the entry point must not be used on a device after
+ * a cudaDeviceReset of it.  Like lapy_pcg_solve it returns once the solve has
+ * finished on `stream`.  All calls share the array and each leaves its
+ * contents behind: calls that overlap on the GPU (two streams or two host
+ * threads) race.  Nothing is allocated or freed. */
 #define LAPY_STATIC_SCRATCH_BYTES ((size_t)32 << 20)
 int lapy_pcg_solve_static(int64_t n, const int32_t* indptr, const int32_t* indices,
                           const double* k_vals, int64_t nnz, int nseg, const int32_t* seg_row,

@@ -129,13 +129,29 @@ def pattern_of(mesh) -> tuple[MeshDevice, FemPattern]:
     return md, pat
 
 
-def assemble(md: MeshDevice, pat: FemPattern, lump: bool, out_dtype=torch.float64, aniso=None):
-    """Numeric assembly: returns (A values on the pattern, M values or M diagonal)."""
+def assemble(md: MeshDevice, pat: FemPattern, lump: bool, out_dtype=torch.float64, aniso=None,
+             seg_elem: torch.Tensor | None = None):
+    """Numeric assembly: returns (A values on the pattern, M values or M diagonal).
+
+    ``seg_elem`` (device int32, nseg+1 element offsets) marks a batch of
+    concatenated meshes: each mesh's degenerate elements are then clamped with
+    its own mean element measure (lapy/solver.py:158-159)."""
     L = _lib.lib()
     s = stream()
     out_f32 = 1 if out_dtype == torch.float32 else 0
     a = torch.empty(pat.nnz, dtype=out_dtype, device="cuda")
     mvals = torch.empty(pat.n if lump else pat.nnz, dtype=out_dtype, device="cuda")
+    if seg_elem is not None:
+        if aniso is not None:
+            raise ValueError("batched assembly has no anisotropic form")
+        nseg = seg_elem.numel() - 1
+        ws = workspace(L.lapy_fem_batch_numeric_workspace_bytes(md.m, md.npe, nseg))
+        _lib.check(L.lapy_fem_batch_numeric(md.npe, dptr(md.v), md.coords_f32, dptr(md.t), md.m, nseg,
+                                            dptr(seg_elem), md.n, dptr(pat.indptr), dptr(pat.indices),
+                                            dptr(pat.seg_ptr), dptr(pat.seg_src), pat.nnz, int(bool(lump)),
+                                            out_f32, dptr(a), dptr(mvals), dptr(ws), ws.numel(), s),
+                   "fem_batch_numeric")
+        return a, mvals
     ws = workspace(L.lapy_fem_numeric_workspace_bytes(md.m, md.npe))
     common = (md.n, dptr(pat.indptr), dptr(pat.indices), dptr(pat.seg_ptr), dptr(pat.seg_src), pat.nnz,
               int(bool(lump)), out_f32, dptr(a), dptr(mvals), dptr(ws), ws.numel(), s)

@@ -65,6 +65,9 @@ _SIGNATURES = {
                                            _i64, _int, _int, _vp, _vp, _vp, _sz, _vp]),
     "lapy_fem_tet_numeric": (_int, [_vp, _int, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _i64, _int, _int,
                                     _vp, _vp, _vp, _sz, _vp]),
+    "lapy_fem_batch_numeric_workspace_bytes": (_sz, [_i64, _int, _int]),
+    "lapy_fem_batch_numeric": (_int, [_int, _vp, _int, _vp, _i64, _int, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _int,
+                                      _int, _vp, _vp, _vp, _sz, _vp]),
     "lapy_csr_diag_index": (_int, [_i64, _vp, _vp, _vp, _vp]),
     "lapy_csr_pattern_map": (_int, [_i64, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
     "lapy_avg_edge_length": (_int, [_vp, _int, _i64, _vp, _vp, C.POINTER(_dbl), _vp, _sz, _vp]),
@@ -174,8 +177,9 @@ def profile_reset() -> None:
 
 def profile_read() -> dict:
     """PCG profile counters (see include/lapy_gb300.h)."""
-    buf = (_dbl * 8)()
-    lib().lapy_profile_read(buf, 8)
     keys = ("pcg_ms", "pcg_launches", "pcg_iterations", "rows", "nnz", "algorithmic_bytes", "lanczos_segment_steps",
-            "second_cgs_passes")
+            "second_cgs_passes", "phase_init_ms", "phase_spmm_ms", "phase_update_ms", "phase_restrict_ms",
+            "phase_coarse_ms", "phase_direction_ms", "phase_final_ms")
+    buf = (_dbl * len(keys))()
+    lib().lapy_profile_read(buf, len(keys))
     return dict(zip(keys, list(buf)))

@@ -168,14 +168,14 @@ __global__ void row_fill_kernel(int64_t n, const int32_t* __restrict__ bucket_pt
 struct NumericWs {
   double* vol;       // m      (element measure in the coordinate type, widened)
   double* partials;  // kVolBlocks
-  double* clamp;     // 1      max(1e-4 * mean(vol), eps)
+  double* clamp;     // max(nseg, 1): max(1e-4 * mean(vol), eps) per mesh
   char* local_a;     // m*L    local stiffness values (output type)
   char* local_m;     // m*L    local mass values (output type)
 };
 constexpr int kVolBlocks = 1024;
 constexpr int kVolThreads = 256;
 
-static size_t numeric_layout(int64_t m, int npe, char* base, NumericWs* ws) {
+static size_t numeric_layout(int64_t m, int npe, int nseg, char* base, NumericWs* ws) {
   const int64_t L = (int64_t)npe * npe;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -185,7 +185,7 @@ static size_t numeric_layout(int64_t m, int npe, char* base, NumericWs* ws) {
   };
   char* p0 = take(sizeof(double) * (size_t)m);
   char* p1 = take(sizeof(double) * kVolBlocks);
-  char* p2 = take(sizeof(double) * 2);
+  char* p2 = take(sizeof(double) * (size_t)std::max(nseg, 2));
   char* p3 = take(sizeof(double) * (size_t)(m * L));
   char* p4 = take(sizeof(double) * (size_t)(m * L));
   if (ws) {
@@ -273,16 +273,54 @@ __global__ void vol_clamp_kernel(const double* __restrict__ partials, int nparts
   }
 }
 
+// Per-mesh clamps of a batch: one block per mesh sums the measures of its
+// element range [seg_elem[s], seg_elem[s+1]) in a fixed order, so that each
+// mesh is clamped with its own mean exactly as a single-mesh assembly does.
 template <typename T>
-__device__ __forceinline__ T clamp_vol(T vol, const double* clamp) {
+__global__ void seg_vol_clamp_kernel(const double* __restrict__ vol, const int32_t* __restrict__ seg_elem,
+                                     double* __restrict__ clamp) {
+  __shared__ double sh[32];
+  const int s = blockIdx.x;
+  const int32_t e0 = seg_elem[s], e1 = seg_elem[s + 1];
+  double acc = 0.0;
+  for (int32_t e = e0 + (int32_t)threadIdx.x; e < e1; e += blockDim.x) acc += vol[e];
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    const T mean = (e1 > e0) ? (T)(acc / (double)(e1 - e0)) : T(0);
+    const T c = T(0.0001) * mean;
+    const double eps = 2.220446049250313e-16;
+    clamp[s] = ((double)c > eps) ? (double)c : eps;
+  }
+}
+
+// Where the clamp of element e comes from: clamp[0] for a single mesh, else
+// the clamp of the mesh whose element range holds e.
+struct ClampDesc {
+  const double* clamp;
+  const int32_t* seg_elem;  // nseg + 1 element offsets (batches), or null
+  int nseg;
+};
+
+template <typename T>
+__device__ __forceinline__ T clamp_vol(T vol, const ClampDesc& cd, int64_t e) {
   const T eps = (T)2.220446049250313e-16;
-  return (vol < eps) ? (T)clamp[0] : vol;
+  if (!(vol < eps)) return vol;
+  int s = 0;
+  if (cd.seg_elem) {  // largest s with seg_elem[s] <= e
+    int lo = 0, hi = cd.nseg - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if ((int64_t)cd.seg_elem[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    s = lo;
+  }
+  return (T)cd.clamp[s];
 }
 
 // Pass 2 (triangles): local stiffness (cotangent) and mass values.
 template <typename T, typename O>
 __global__ void tria_local_kernel(const T* __restrict__ v, const int32_t* __restrict__ t, int64_t m,
-                                  const double* __restrict__ clamp, int lump,
+                                  const ClampDesc clamp, int lump,
                                   O* __restrict__ la, O* __restrict__ lm) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m) return;
@@ -290,7 +328,7 @@ __global__ void tria_local_kernel(const T* __restrict__ v, const int32_t* __rest
   const V3<T> v2mv1 = sub(v2, v1), v3mv2 = sub(v3, v2), v1mv3 = sub(v1, v3);
   const V3<T> cr = cross3(v3mv2, v1mv3);
   T vol = T(2) * sqrt(dot3(cr, cr));
-  vol = clamp_vol(vol, clamp);
+  vol = clamp_vol(vol, clamp, e);
   // solver.py:163-169
   const T a12 = dot3(v3mv2, v1mv3) / vol;
   const T a23 = dot3(v1mv3, v2mv1) / vol;
@@ -325,7 +363,7 @@ __global__ void tria_aniso_local_kernel(const T* __restrict__ v, const int32_t* 
                                         int64_t m, const double* __restrict__ u1,
                                         const double* __restrict__ u2,
                                         const double* __restrict__ an,
-                                        const double* __restrict__ clamp, int lump,
+                                        const ClampDesc clamp, int lump,
                                         O* __restrict__ la, O* __restrict__ lm) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m) return;
@@ -340,7 +378,7 @@ __global__ void tria_aniso_local_kernel(const T* __restrict__ v, const int32_t* 
   const double p13[2] = {dot3(U1, d13), dot3(U2, d13)};
   const V3<T> cr = cross3(v3mv2, v1mv3);
   T vol = T(2) * sqrt(dot3(cr, cr));
-  vol = clamp_vol(vol, clamp);
+  vol = clamp_vol(vol, clamp, e);
   const double a0 = an[2 * e], a1 = an[2 * e + 1];
   const double dv = (double)vol;
   // np.sum(x * aniso_mat * y, axis=1) = (x0*a0)*y0 + (x1*a1)*y1
@@ -371,7 +409,7 @@ __global__ void tria_aniso_local_kernel(const T* __restrict__ v, const int32_t* 
 // Pass 2 (tetrahedra, solver.py:426-532).
 template <typename T, typename O>
 __global__ void tet_local_kernel(const T* __restrict__ v, const int32_t* __restrict__ t, int64_t m,
-                                 const double* __restrict__ clamp, int lump, O* __restrict__ la,
+                                 const ClampDesc clamp, int lump, O* __restrict__ la,
                                  O* __restrict__ lm) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m) return;
@@ -381,7 +419,7 @@ __global__ void tet_local_kernel(const T* __restrict__ v, const int32_t* __restr
               e5 = sub(v4, v2), e6 = sub(v4, v3);
   const V3<T> cr = cross3(e1, e3);
   T vol = abs(dot3(e4, cr));
-  vol = clamp_vol(vol, clamp);
+  vol = clamp_vol(vol, clamp, e);
   const T e11 = dot3(e1, e1), e22 = dot3(e2, e2), e33 = dot3(e3, e3), e44 = dot3(e4, e4),
           e55 = dot3(e5, e5), e66 = dot3(e6, e6);
   const T e12 = dot3(e1, e2), e13 = dot3(e1, e3), e14 = dot3(e1, e4), e15 = dot3(e1, e5),
@@ -548,7 +586,12 @@ extern "C" int lapy_csr_symbolic_fill(const int32_t* elems, int64_t m, int npe, 
 
 extern "C" size_t lapy_fem_numeric_workspace_bytes(int64_t m, int npe) {
   if (m < 0 || (npe != 3 && npe != 4)) return 0;
-  return numeric_layout(m, npe, nullptr, nullptr) + 256;
+  return numeric_layout(m, npe, 1, nullptr, nullptr) + 256;
+}
+
+extern "C" size_t lapy_fem_batch_numeric_workspace_bytes(int64_t m, int npe, int nseg) {
+  if (m < 0 || (npe != 3 && npe != 4) || nseg < 1) return 0;
+  return numeric_layout(m, npe, nseg, nullptr, nullptr) + 256;
 }
 
 namespace {
@@ -560,7 +603,7 @@ int fem_numeric_impl(ElemKind kind, const T* v, const int32_t* t, int64_t m, con
                      const double* u2, const double* an, int64_t n, const int32_t* indptr,
                      const int32_t* indices, const int32_t* seg_ptr, const int32_t* seg_src,
                      int64_t nnz, int lump, O* a_vals, O* m_vals, const NumericWs& ws,
-                     cudaStream_t stream) {
+                     int nseg, const int32_t* seg_elem, cudaStream_t stream) {
   const int npe = (kind == ElemKind::Tet) ? 4 : 3;
   const unsigned vb = (unsigned)std::min<int64_t>(kVolBlocks, std::max<int64_t>(1, lapy_ceil_div(m, kVolThreads)));
   if (npe == 3)
@@ -568,17 +611,24 @@ int fem_numeric_impl(ElemKind kind, const T* v, const int32_t* t, int64_t m, con
   else
     elem_vol_kernel<T, 4><<<vb, kVolThreads, 0, stream>>>(v, t, m, ws.vol, ws.partials);
   LAPY_TRY(lapy_check_launch("elem_vol_kernel"));
-  vol_clamp_kernel<T><<<1, 256, 0, stream>>>(ws.partials, (int)vb, m, ws.clamp);
-  LAPY_TRY(lapy_check_launch("vol_clamp_kernel"));
+  ClampDesc cd{ws.clamp, nullptr, 1};
+  if (seg_elem) {
+    seg_vol_clamp_kernel<T><<<nseg, 256, 0, stream>>>(ws.vol, seg_elem, ws.clamp);
+    LAPY_TRY(lapy_check_launch("seg_vol_clamp_kernel"));
+    cd = ClampDesc{ws.clamp, seg_elem, nseg};
+  } else {
+    vol_clamp_kernel<T><<<1, 256, 0, stream>>>(ws.partials, (int)vb, m, ws.clamp);
+    LAPY_TRY(lapy_check_launch("vol_clamp_kernel"));
+  }
   O* la = (O*)ws.local_a;
   O* lm = (O*)ws.local_m;
   const unsigned eb = lapy_ceil_div(m, 128);
   if (kind == ElemKind::Tria)
-    tria_local_kernel<T, O><<<eb, 128, 0, stream>>>(v, t, m, ws.clamp, lump, la, lm);
+    tria_local_kernel<T, O><<<eb, 128, 0, stream>>>(v, t, m, cd, lump, la, lm);
   else if (kind == ElemKind::TriaAniso)
-    tria_aniso_local_kernel<T, O><<<eb, 128, 0, stream>>>(v, t, m, u1, u2, an, ws.clamp, lump, la, lm);
+    tria_aniso_local_kernel<T, O><<<eb, 128, 0, stream>>>(v, t, m, u1, u2, an, cd, lump, la, lm);
   else
-    tet_local_kernel<T, O><<<eb, 128, 0, stream>>>(v, t, m, ws.clamp, lump, la, lm);
+    tet_local_kernel<T, O><<<eb, 128, 0, stream>>>(v, t, m, cd, lump, la, lm);
   LAPY_TRY(lapy_check_launch("elem_local_kernel"));
   segmented_reduce_kernel<O><<<lapy_ceil_div(nnz, 256), 256, 0, stream>>>(
       nnz, seg_ptr, seg_src, la, lm, a_vals, lump ? nullptr : m_vals);
@@ -595,7 +645,8 @@ int fem_numeric_dispatch(ElemKind kind, const void* v, int coords_f32, const int
                          const void* u1, const void* u2, const void* an, int64_t n,
                          const int32_t* indptr, const int32_t* indices, const int32_t* seg_ptr,
                          const int32_t* seg_src, int64_t nnz, int lump, int out_f32, void* a_vals,
-                         void* m_vals, void* work, size_t ws_bytes, void* stream_) {
+                         void* m_vals, void* work, size_t ws_bytes, void* stream_, int nseg = 1,
+                         const int32_t* seg_elem = nullptr) {
   cudaStream_t stream = (cudaStream_t)stream_;
   const int npe = (kind == ElemKind::Tet) ? 4 : 3;
   if (!v || !t || m <= 0 || n <= 0 || nnz <= 0 || !indptr || !indices || !seg_ptr || !seg_src ||
@@ -607,10 +658,14 @@ int fem_numeric_dispatch(ElemKind kind, const void* v, int coords_f32, const int
     lapy_set_last_message("fem_tria_aniso_numeric: u1, u2 and aniso_mat are required");
     return LAPY_ERR_INVALID;
   }
-  if (ws_bytes < lapy_fem_numeric_workspace_bytes(m, npe)) return LAPY_ERR_WORKSPACE;
+  if (nseg < 1 || (seg_elem == nullptr && nseg != 1)) {
+    lapy_set_last_message("fem_numeric: nseg must be >= 1, with seg_elem for nseg > 1");
+    return LAPY_ERR_INVALID;
+  }
+  if (ws_bytes < lapy_fem_batch_numeric_workspace_bytes(m, npe, nseg)) return LAPY_ERR_WORKSPACE;
   NumericWs ws;
   char* base = (char*)(((uintptr_t)work + 255) & ~uintptr_t(255));
-  numeric_layout(m, npe, base, &ws);
+  numeric_layout(m, npe, nseg, base, &ws);
   const double* U1 = (const double*)u1;
   const double* U2 = (const double*)u2;
   const double* AN = (const double*)an;
@@ -618,18 +673,18 @@ int fem_numeric_dispatch(ElemKind kind, const void* v, int coords_f32, const int
     if (out_f32)
       return fem_numeric_impl<float, float>(kind, (const float*)v, t, m, U1, U2, AN, n, indptr,
                                             indices, seg_ptr, seg_src, nnz, lump, (float*)a_vals,
-                                            (float*)m_vals, ws, stream);
+                                            (float*)m_vals, ws, nseg, seg_elem, stream);
     return fem_numeric_impl<float, double>(kind, (const float*)v, t, m, U1, U2, AN, n, indptr,
                                            indices, seg_ptr, seg_src, nnz, lump, (double*)a_vals,
-                                           (double*)m_vals, ws, stream);
+                                           (double*)m_vals, ws, nseg, seg_elem, stream);
   }
   if (out_f32)
     return fem_numeric_impl<double, float>(kind, (const double*)v, t, m, U1, U2, AN, n, indptr,
                                            indices, seg_ptr, seg_src, nnz, lump, (float*)a_vals,
-                                           (float*)m_vals, ws, stream);
+                                           (float*)m_vals, ws, nseg, seg_elem, stream);
   return fem_numeric_impl<double, double>(kind, (const double*)v, t, m, U1, U2, AN, n, indptr,
                                           indices, seg_ptr, seg_src, nnz, lump, (double*)a_vals,
-                                          (double*)m_vals, ws, stream);
+                                          (double*)m_vals, ws, nseg, seg_elem, stream);
 }
 
 }  // namespace
@@ -664,4 +719,18 @@ extern "C" int lapy_fem_tet_numeric(const void* v, int coords_f32, const int32_t
   return fem_numeric_dispatch(ElemKind::Tet, v, coords_f32, t, m, nullptr, nullptr, nullptr, n,
                               indptr, indices, seg_ptr, seg_src, nnz, lump, out_f32, a_vals, m_vals,
                               work, ws_bytes, stream);
+}
+
+extern "C" int lapy_fem_batch_numeric(int npe, const void* v, int coords_f32, const int32_t* t, int64_t m,
+                                      int nseg, const int32_t* seg_elem, int64_t n, const int32_t* indptr,
+                                      const int32_t* indices, const int32_t* seg_ptr, const int32_t* seg_src,
+                                      int64_t nnz, int lump, int out_f32, void* a_vals, void* m_vals, void* work,
+                                      size_t ws_bytes, void* stream) {
+  if ((npe != 3 && npe != 4) || nseg < 1 || !seg_elem) {
+    lapy_set_last_message("fem_batch_numeric: npe must be 3 or 4, nseg >= 1 and seg_elem given");
+    return LAPY_ERR_INVALID;
+  }
+  return fem_numeric_dispatch(npe == 4 ? ElemKind::Tet : ElemKind::Tria, v, coords_f32, t, m, nullptr, nullptr,
+                              nullptr, n, indptr, indices, seg_ptr, seg_src, nnz, lump, out_f32, a_vals, m_vals,
+                              work, ws_bytes, stream, nseg, seg_elem);
 }

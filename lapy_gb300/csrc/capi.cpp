@@ -42,8 +42,11 @@ static std::atomic<long long> g_launches{0};
 static std::mutex g_prof_mu;
 static bool g_prof_on = false;
 // pcg_ms, pcg_solves, pcg_iters, rows, nnz, bytes (algorithmic),
-// Lanczos (segment, block step) pairs, of which with a second CGS pass
-static double g_prof[8] = {0};
+// Lanczos (segment, block step) pairs, of which with a second CGS pass,
+// then the PCG's per-phase milliseconds (kPcgPhases slots)
+constexpr int kPcgPhases = LAPY_PCG_PHASES;
+constexpr int kProfSlots = 8 + kPcgPhases;
+static double g_prof[kProfSlots] = {0};
 
 void lapy_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 bool lapy_profile_enabled() { return g_prof_on; }
@@ -59,6 +62,11 @@ void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long 
   // touched: matrix (value + column index per nonzero, row pointer per row),
   // 11 vector streams of p values and 2 of the Jacobi diagonal
   g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (4 + 11.0 * p * eb + 2.0 * eb);
+}
+
+void lapy_profile_add_phases(const double* ms) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  for (int k = 0; k < kPcgPhases; ++k) g_prof[8 + k] += ms[k];
 }
 
 void lapy_profile_add_reorth(long long steps, long long second_passes) {
@@ -81,7 +89,7 @@ extern "C" void lapy_profile_reset(void) {
 
 extern "C" int lapy_profile_read(double* out, int n) {
   std::lock_guard<std::mutex> lock(g_prof_mu);
-  for (int i = 0; i < n && i < 8; ++i) out[i] = g_prof[i];
+  for (int i = 0; i < n && i < kProfSlots; ++i) out[i] = g_prof[i];
   return 0;
 }
 

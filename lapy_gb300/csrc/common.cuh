@@ -30,6 +30,12 @@ void lapy_count_launch();
 bool lapy_profile_enabled();
 void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int elem_bytes);
 void lapy_profile_add_reorth(long long steps, long long second_passes);
+// Per-phase device time of the persistent PCG (profile mode): the interval
+// between consecutive grid-barrier exits, accumulated per phase: initialisation,
+// SpMM (Q = K P), update (X, R), coarse restriction, coarse solve, direction
+// update, final publication.
+constexpr int kPcgPhases = LAPY_PCG_PHASES;
+void lapy_profile_add_phases(const double* ms);
 
 static inline int lapy_check_launch(const char* what) {
   lapy_count_launch();

@@ -223,7 +223,14 @@ struct PcgArgs {
   double rtol2_64;
   S delta2;
   int ru_every;
+  unsigned long long* phase_ns;  // [kPcgPhases] device time per phase (profile mode), or null
 };
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // NP consecutive values of row `row` (vectorised: rows are NP * sizeof(V)
 // aligned because every buffer starts on a 256-byte boundary).
@@ -674,6 +681,18 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
   if (threadIdx.x == 0) s_act = 0;
   // rows and nonzeros this warp streamed through the SpMM phase
   unsigned long long w_rows = 0, w_nnz = 0;
+  // profile mode: thread 0 of CTA 0 adds the device time between consecutive
+  // barrier exits to the phase that just ended (a barrier exit marks the
+  // moment the slowest CTA finished the phase)
+  const bool timer = a.phase_ns != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long t_mark = timer ? globaltimer_ns() : 0ull;
+  auto mark = [&](int ph) {
+    if (timer) {
+      const unsigned long long now = globaltimer_ns();
+      a.phase_ns[ph] += now - t_mark;
+      t_mark = now;
+    }
+  };
 
   // ---- phase 0: X = 0, R = B, P = M^-1 R (Jacobi); partial b'b and r'z
   FOR_MY_PIECES(a, {
@@ -786,6 +805,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     }
   })
   if (!grid_sync(a.bar, &s_act, &s_seen)) return;
+  mark(0);
   unsigned seen_prev = s_seen, nact = s_seen;
 
   int it = 0;
@@ -878,6 +898,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
           fold_pieces<V, NP>(a, part_rz, slot_rz);
         }
         if (!grid_sync(a.bar)) return;
+        mark(2);
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.n_updates, 1u);
       }
     }
@@ -949,6 +970,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       fold_pieces<V, NP>(a, part_pq, slot_pq);
     }
     if (!grid_sync(a.bar)) return;
+    mark(1);
 
     // ---- phase B: alpha, X += alpha P, R -= alpha Q, partial r'r (and r'z for Jacobi)
     FOR_MY_PIECES(a, {
@@ -999,13 +1021,16 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       if (kDiagPC) fold_pieces<V, NP>(a, part_rz, slot_rz);
     }
     if (!grid_sync(a.bar)) return;
+    mark(2);
 
     if constexpr (PC == kPrecTwoLevel) {
       // ---- phases R, G: coarse correction of the new residual
       coarse_restrict<V, NP>(a, st_cur, false);
       if (!grid_sync(a.bar)) return;
+      mark(3);
       coarse_solve<V, NP>(a, st_cur, false);
       if (!grid_sync(a.bar)) return;
+      mark(4);
     }
 
     if constexpr (PC == kPrecFactored) {
@@ -1025,6 +1050,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
         fold_pieces<V, NP>(a, part_rz, slot_rz);
       }
       if (!grid_sync(a.bar)) return;
+      mark(3);
     }
 
     // ---- phase C: convergence, beta, P = Z + beta P
@@ -1096,6 +1122,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       }
     })
     if (!grid_sync(a.bar, &s_act, &s_seen)) return;
+    mark(5);
     nact = s_seen - seen_prev;
     seen_prev = s_seen;
   }
@@ -1125,6 +1152,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     }
   })
   if (blockIdx.x == 0 && threadIdx.x == 0) a.iters[0] = it;
+  mark(6);
   if (lane == 0 && w_rows != 0) {
     atomicAdd(&a.work[0], w_rows);
     atomicAdd(&a.work[1], w_nnz);
@@ -1317,7 +1345,9 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.bb = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
   a.state = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
   // control words: [2] iters, [5] err, [6..9] work (u64 x2), [10..11] ru_flag,
-  // [12] updates; the barrier word sits alone on the next 128-byte line
+  // [12] updates, [14..27] phase times (u64 x kPcgPhases); the barrier word
+  // sits alone on the next 128-byte line
+  static_assert(14 + 2 * kPcgPhases <= 32, "phase timers overlap the barrier line");
   unsigned* ctl = (unsigned*)w;
   w += a256(256);
   a.iters = (int*)(ctl + 2);
@@ -1362,6 +1392,7 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   LAPY_CUDA_TRY(cudaMemsetAsync(state_dev, 0, sizeof(int32_t) * (size_t)ct.nseg * p, stream));
   int st;
   const bool prof = lapy_profile_enabled();
+  a.phase_ns = prof ? (unsigned long long*)(ctl + 14) : nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (prof) {
     LAPY_CUDA_TRY(cudaEventCreate(&e0));
@@ -1393,7 +1424,7 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   }
   if (st != LAPY_OK) return st;
   if (prof) LAPY_CUDA_TRY(cudaEventRecord(e1, stream));
-  unsigned hctl[16];
+  unsigned hctl[32];
   LAPY_CUDA_TRY(cudaMemcpyAsync(hctl, ctl, sizeof(hctl), cudaMemcpyDeviceToHost, stream));
   LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
   if (prof) {
@@ -1405,6 +1436,13 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
     memcpy(&rows, &hctl[6], 8);
     memcpy(&nnz, &hctl[8], 8);
     lapy_profile_add_pcg(ms, (long long)hctl[2], (long long)rows, (long long)nnz, p, (int)sizeof(V));
+    double phase_ms[kPcgPhases];
+    for (int k = 0; k < kPcgPhases; ++k) {
+      unsigned long long ns;
+      memcpy(&ns, &hctl[14 + 2 * k], 8);
+      phase_ms[k] = (double)ns * 1e-6;
+    }
+    lapy_profile_add_phases(phase_ms);
   }
   if (hctl[5] != 0) {
     lapy_set_last_message("pcg: grid barrier timed out");

@@ -92,7 +92,7 @@ class BatchInput:
         if not meshes:
             raise ValueError("empty batch")
         npe = meshes[0].t.shape[1]
-        vs, ts, seg = [], [], [0]
+        vs, ts, seg, segel = [], [], [0], [0]
         f32 = all(np.asarray(m.v).dtype == np.float32 for m in meshes)
         for m in meshes:
             t = np.asarray(m.t)
@@ -104,6 +104,7 @@ class BatchInput:
             vs.append(np.asarray(m.v, dtype=np.float32 if f32 else np.float64))
             ts.append(t.astype(np.int64) + seg[-1])
             seg.append(seg[-1] + nv)
+            segel.append(segel[-1] + len(t))
         if seg[-1] >= 2**31:
             raise ValueError("batch exceeds the int32 index range")
         v = torch.from_numpy(np.ascontiguousarray(np.concatenate(vs))).to("cuda")
@@ -111,19 +112,21 @@ class BatchInput:
         self.mesh = MeshDevice(v, t, seg[-1], seg[-1], t.shape[0], npe)
         self.seg_row = np.array(seg, dtype=np.int32)
         self.seg_row_dev = torch.from_numpy(self.seg_row).to("cuda")
+        self.seg_elem = np.array(segel, dtype=np.int32)
+        self.seg_elem_dev = torch.from_numpy(self.seg_elem).to("cuda")
 
 
 class BatchedFEM:
     """Block-diagonal stiffness and mass of a batch, assembled on the device.
 
-    The element-measure clamp of the reference (lapy/solver.py:158-159) uses
-    the mean over the whole batch here; it only changes elements whose
-    measure is below machine epsilon."""
+    Each mesh's degenerate elements are clamped with that mesh's own mean
+    element measure, as a separate ``Solver`` per mesh would
+    (lapy/solver.py:158-159)."""
 
     def __init__(self, meshes=None, lump: bool = False, _input: BatchInput | None = None):
         inp = _input if _input is not None else BatchInput(meshes)
         pat = build_pattern(inp.mesh)
-        a, m = assemble(inp.mesh, pat, lump)
+        a, m = assemble(inp.mesh, pat, lump, seg_elem=inp.seg_elem_dev)
         self.input = inp
         self.pattern = pat
         self.seg_row = inp.seg_row

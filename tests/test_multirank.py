@@ -78,4 +78,5 @@ def test_reference_arm_json_contract():
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     cb = line["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"]
-    assert "workload" in line["config"]
+    assert cb["cpu_model"] and line["ms_per_step"] > 0
+    assert line["config"]["workload"].startswith("batched ShapeDNA: 8 deformed icospheres")
