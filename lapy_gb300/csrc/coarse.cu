@@ -7,12 +7,14 @@
 // on a fixed set of host threads).  Device: the Galerkin matrix W'KW of every
 // segment (one thread per coarse row, fixed summation order) and its dense
 // inverse (one CTA per segment: FP64 Cholesky, triangular inverse, B'B),
-// stored in FP32 for the per-iteration coarse product of the PCG.
+// split into its dominant rank-1 term (FP32) and a BF16 remainder for the
+// per-iteration coarse product of the PCG.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <thread>
 #include <vector>
+#include <cuda_bf16.h>
 #include "coarse.cuh"
 
 namespace lapy {
@@ -37,22 +39,30 @@ int64_t two_level_max_aggs(const int32_t* seg_row, int nseg) {
   return t;
 }
 
-static int64_t max_coarse_entries(const int32_t* seg_row, int nseg) {
-  int64_t t = 0;
+__host__ __device__ static inline int64_t pad8(int64_t c) { return (c + 7) & ~int64_t(7); }
+
+// Bounds over all segments: coarse entries (square blocks), padded BF16
+// entries (rows rounded up to 8), and coarse-solve tasks.
+static void coarse_bounds(const int32_t* seg_row, int nseg, int64_t* ne, int64_t* ne_pad, int64_t* ntask) {
+  *ne = *ne_pad = *ntask = 0;
   for (int s = 0; s < nseg; ++s) {
     const int64_t c = std::min<int64_t>(seg_cap(seg_row[s + 1] - seg_row[s]), kCoarseMaxDim);
-    t += c * c;
+    *ne += c * c;
+    *ne_pad += c * pad8(c);
+    *ntask += (c + kCoarseTaskRows - 1) / kCoarseTaskRows;
   }
-  return t;
 }
 
 size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg, int nvc) {
   const int64_t na = two_level_max_aggs(seg_row, nseg);
-  const int64_t ne = max_coarse_entries(seg_row, nseg);
+  int64_t ne, ne_pad, nt;
+  coarse_bounds(seg_row, nseg, &ne, &ne_pad, &nt);
   return a256(4 * (size_t)n) * 2 + a256(4 * (size_t)(na + 1)) + a256(4 * (size_t)na) +
-         a256(4 * (size_t)(nseg + 1)) + a256(8 * (size_t)(nseg + 1)) + a256(4 * (size_t)ne) +
-         a256(8 * (size_t)ne) + a256(4 * (size_t)nseg) + a256(4 * (size_t)(std::max(nvc, 1) + 1)) +
-         a256(4 * (size_t)(nseg + 1)) + a256(4 * (size_t)std::max(nseg, 1)) + 1024;
+         a256(4 * (size_t)(nseg + 1)) + a256(8 * (size_t)(nseg + 1)) + a256(2 * (size_t)ne_pad) +
+         2 * a256(8 * (size_t)ne) + a256(4 * (size_t)nseg) + a256(4 * (size_t)(std::max(nvc, 1) + 1)) * 2 +
+         a256(4 * (size_t)(nseg + 1)) + a256(4 * (size_t)std::max(nseg, 1)) + a256(4 * (size_t)na) +
+         a256(4 * (size_t)std::max(nseg, 1)) + 3 * a256(4 * (size_t)std::max<int64_t>(nt, 1)) +
+         a256(8 * (size_t)(nseg + 1)) + 2048;
 }
 
 // ---- host aggregation -------------------------------------------------------
@@ -164,25 +174,46 @@ __global__ void coarse_galerkin_kernel(int nagg, const int32_t* __restrict__ agg
 }
 
 constexpr int kInvThreads = 512;
+// Power iterations for the dominant eigenvector of the coarse inverse: the
+// smallest eigenvalue of W'KW is the shifted constant mode, separated from
+// the next by two to four orders of magnitude on mesh systems, so a few
+// iterations give it to working precision; the split below stays exact for
+// any v (R is formed from the same v), only the size of R depends on it.
+constexpr int kPowerIters = 12;
+
+__device__ __forceinline__ uint16_t to_bf16_bits(double x) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn((float)x));
+}
 
 // In-place inverse of one SPD block A (nc x nc, row-major, FP64) per CTA:
 // A = L L' (lower triangle), B = L^-1 kept transposed in the strict upper
-// triangle with its diagonal in shared memory, then A^-1 = B'B written to
-// `out` in FP32.  A non-positive pivot leaves the segment's block zero (no
-// coarse correction: the preconditioner falls back to Jacobi there).
+// triangle with its diagonal in shared memory, then F = A^-1 = B'B (FP64,
+// full) into `full`.  Then the dominant eigenpair of F by power iteration,
+// v (unit) and c = v'Fv, and the split F = c v v' + R: v and c in FP32, R in
+// BF16 (rows padded to ld = nc rounded up to 8).  A non-positive pivot leaves
+// the segment's block zero (no coarse correction: the preconditioner falls
+// back to Jacobi there).
 __global__ void __launch_bounds__(kInvThreads) coarse_inverse_kernel(const int32_t* __restrict__ seg_agg,
                                                                      const int64_t* __restrict__ off,
+                                                                     const int64_t* __restrict__ off_pad,
                                                                      double* __restrict__ kc,
-                                                                     float* __restrict__ out,
+                                                                     double* __restrict__ full,
+                                                                     uint16_t* __restrict__ out,
+                                                                     float* __restrict__ kvec,
+                                                                     float* __restrict__ kscale,
                                                                      int* __restrict__ failed) {
   __shared__ double col[kCoarseMaxDim];
   __shared__ double diagb[kCoarseMaxDim];
+  __shared__ double red[32];
   __shared__ int ok;
   const int s = blockIdx.x;
-  const int nc = seg_agg[s + 1] - seg_agg[s];
+  const int base = seg_agg[s];
+  const int nc = seg_agg[s + 1] - base;
   if (nc <= 0) return;
+  const int64_t ld = pad8(nc);
   double* A = kc + off[s];
-  float* O = out + off[s];
+  double* F = full + off[s];
+  uint16_t* O = out + off_pad[s];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = kInvThreads / 32;
   if (tid == 0) ok = 1;
   __syncthreads();
@@ -212,8 +243,12 @@ __global__ void __launch_bounds__(kInvThreads) coarse_inverse_kernel(const int32
     __syncthreads();
   }
   if (!ok) {
-    for (int64_t t = tid; t < (int64_t)nc * nc; t += kInvThreads) O[t] = 0.0f;
-    if (tid == 0) failed[s] = 1;
+    for (int64_t t = tid; t < (int64_t)nc * ld; t += kInvThreads) O[t] = 0;
+    for (int i = tid; i < nc; i += kInvThreads) kvec[base + i] = 0.0f;
+    if (tid == 0) {
+      kscale[s] = 0.0f;
+      failed[s] = 1;
+    }
     return;
   }
   // B = L^-1: row c of U (= column c of B) lives in A[c][c+1..nc), B[c][c] in diagb
@@ -251,10 +286,45 @@ __global__ void __launch_bounds__(kInvThreads) coarse_inverse_kernel(const int32
       }
       acc = warp_sum(acc);
       if (lane == 0) {
-        O[(int64_t)a * nc + b] = (float)acc;
-        O[(int64_t)b * nc + a] = (float)acc;
+        F[(int64_t)a * nc + b] = acc;
+        F[(int64_t)b * nc + a] = acc;
       }
     }
+  }
+  // dominant eigenvector of F: v <- F v / ||F v|| (v in col, F v in diagb)
+  double* v = col;
+  double* y = diagb;
+  auto matvec = [&]() {  // y = F v, one warp per row
+    __syncthreads();
+    for (int a = warp; a < nc; a += nwarp) {
+      const double* Fa = F + (int64_t)a * nc;
+      double acc = 0.0;
+      for (int b = lane; b < nc; b += 32) acc += Fa[b] * v[b];
+      acc = warp_sum(acc);
+      if (lane == 0) y[a] = acc;
+    }
+    __syncthreads();
+  };
+  for (int i = tid; i < nc; i += kInvThreads) v[i] = 1.0;
+  for (int it = 0; it < kPowerIters; ++it) {
+    matvec();
+    double part = 0.0;
+    for (int i = tid; i < nc; i += kInvThreads) part += y[i] * y[i];
+    const double nrm = sqrt(block_sum(part, red));
+    for (int i = tid; i < nc; i += kInvThreads) v[i] = y[i] / nrm;
+  }
+  matvec();
+  double part = 0.0;
+  for (int i = tid; i < nc; i += kInvThreads) part += v[i] * y[i];
+  const double c = block_sum(part, red);  // v'Fv
+  for (int i = tid; i < nc; i += kInvThreads) kvec[base + i] = (float)v[i];
+  if (tid == 0) kscale[s] = (float)c;
+  // R = F - c v v' in BF16, rows padded with zeros to ld
+  for (int a = warp; a < nc; a += nwarp) {
+    const double* Fa = F + (int64_t)a * nc;
+    uint16_t* Oa = O + (int64_t)a * ld;
+    const double cva = c * v[a];
+    for (int b = lane; b < ld; b += 32) Oa[b] = (b < nc) ? to_bf16_bits(Fa[b] - cva * v[b]) : (uint16_t)0;
   }
 }
 
@@ -284,10 +354,11 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
     for (auto& th : pool) th.join();
   }
   std::vector<int32_t> seg_agg(nseg + 1, 0);
-  std::vector<int64_t> off(nseg + 1, 0);
+  std::vector<int64_t> off(nseg + 1, 0), off_pad(nseg + 1, 0);
   for (int s = 0; s < nseg; ++s) {
     seg_agg[s + 1] = seg_agg[s] + nc[s];
     off[s + 1] = off[s] + (int64_t)nc[s] * nc[s];
+    off_pad[s + 1] = off_pad[s] + (int64_t)nc[s] * pad8(nc[s]);
   }
   const int nagg = seg_agg[nseg];
   std::vector<int32_t> agg(n, -1), agg_sid(nagg), agg_ptr(nagg + 1, 0), agg_row;
@@ -306,15 +377,38 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
       if (agg[v] >= 0) agg_row[fill[agg[v]]++] = (int32_t)v;
   }
 
-  // the coarse work (a restriction over the aggregate's rows and one row of
-  // the segment's dense inverse per aggregate) split over the virtual CTAs in
-  // contiguous ranges of equal aggregate counts (the time of a coarse row is
-  // mostly the latency of its dependent loads and warp reductions, so counts
-  // balance better than bytes), and the reduction slots of each segment's
-  // coarse partial sums
+  // coarse-solve tasks (up to kCoarseTaskRows coarse rows of one segment),
+  // split over the virtual CTAs in contiguous ranges of about equal cost (the
+  // BF16 entries they stream, plus a fixed cost per row and per task); the
+  // aggregates of a virtual CTA's tasks are also its share of the
+  // restriction, and the reduction slots of each segment's coarse partial
+  // sums follow from that split
+  std::vector<int32_t> task_seg, task_g0, task_g1;
+  std::vector<double> task_cost;
+  for (int s = 0; s < nseg; ++s)
+    for (int g = seg_agg[s]; g < seg_agg[s + 1]; g += kCoarseTaskRows) {
+      const int g1 = std::min(g + kCoarseTaskRows, seg_agg[s + 1]);
+      task_seg.push_back(s);
+      task_g0.push_back(g);
+      task_g1.push_back(g1);
+      task_cost.push_back((double)(g1 - g) * (double)(pad8(nc[s]) + 64) + 512.0);
+    }
+  const int ntask = (int)task_seg.size();
+  std::vector<int32_t> vc_task(nvc + 1, 0);
+  {
+    double total = 0.0;
+    for (double c : task_cost) total += c;
+    double acc = 0.0;
+    int v = 1;
+    for (int t = 0; t < ntask; ++t) {
+      acc += task_cost[t];
+      while (v < nvc && acc >= total * v / nvc) vc_task[v++] = t + 1;
+    }
+    while (v <= nvc) vc_task[v++] = ntask;
+  }
   std::vector<int32_t> vc_agg(nvc + 1, 0), seg_aslot(nseg + 1, 0), seg_avc0(std::max(nseg, 1), 0);
   {
-    for (int v = 0; v <= nvc; ++v) vc_agg[v] = (int32_t)((int64_t)nagg * v / nvc);
+    for (int v = 0; v <= nvc; ++v) vc_agg[v] = vc_task[v] < ntask ? task_g0[vc_task[v]] : nagg;
     auto vc_of = [&](int32_t g) {
       return (int)(std::upper_bound(vc_agg.begin(), vc_agg.end(), g) - vc_agg.begin()) - 1;
     };
@@ -331,8 +425,9 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   // device layout
   char* w = (char*)(((uintptr_t)mem + 255) & ~uintptr_t(255));
   const int64_t na_max = two_level_max_aggs(seg_row, nseg);
-  const int64_t ne_max = max_coarse_entries(seg_row, nseg);
-  if (nagg > na_max || off[nseg] > ne_max) {
+  int64_t ne_max, ne_pad_max, nt_max;
+  coarse_bounds(seg_row, nseg, &ne_max, &ne_pad_max, &nt_max);
+  if (nagg > na_max || off[nseg] > ne_max || off_pad[nseg] > ne_pad_max || ntask > nt_max) {
     lapy_set_last_message("two-level: coarse space exceeds its bound");
     return LAPY_ERR_WORKSPACE;
   }
@@ -342,11 +437,19 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   int32_t* d_sid = (int32_t*)w; w += a256(4 * (size_t)na_max);
   int32_t* d_seg = (int32_t*)w; w += a256(4 * (size_t)(nseg + 1));
   int64_t* d_off = (int64_t*)w; w += a256(8 * (size_t)(nseg + 1));
-  float* d_kinv = (float*)w; w += a256(4 * (size_t)ne_max);
+  uint16_t* d_kinv = (uint16_t*)w; w += a256(2 * (size_t)ne_pad_max);
   double* d_kc = (double*)w; w += a256(8 * (size_t)ne_max);
+  double* d_full = (double*)w; w += a256(8 * (size_t)ne_max);
   int32_t* d_vca = (int32_t*)w; w += a256(4 * (size_t)(nvc + 1));
   int32_t* d_asl = (int32_t*)w; w += a256(4 * (size_t)(nseg + 1));
   int32_t* d_av0 = (int32_t*)w; w += a256(4 * (size_t)std::max(nseg, 1));
+  float* d_kvec = (float*)w; w += a256(4 * (size_t)na_max);
+  float* d_kscale = (float*)w; w += a256(4 * (size_t)std::max(nseg, 1));
+  int32_t* d_tseg = (int32_t*)w; w += a256(4 * (size_t)std::max<int64_t>(nt_max, 1));
+  int32_t* d_tg0 = (int32_t*)w; w += a256(4 * (size_t)std::max<int64_t>(nt_max, 1));
+  int32_t* d_tg1 = (int32_t*)w; w += a256(4 * (size_t)std::max<int64_t>(nt_max, 1));
+  int32_t* d_vct = (int32_t*)w; w += a256(4 * (size_t)(nvc + 1));
+  int64_t* d_offp = (int64_t*)w; w += a256(8 * (size_t)(nseg + 1));
   int* d_fail = (int*)w;
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_agg, agg.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
   if (!agg_row.empty())
@@ -359,13 +462,21 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_vca, vc_agg.data(), 4 * vc_agg.size(), cudaMemcpyHostToDevice, stream));
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_asl, seg_aslot.data(), 4 * seg_aslot.size(), cudaMemcpyHostToDevice, stream));
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_av0, seg_avc0.data(), 4 * seg_avc0.size(), cudaMemcpyHostToDevice, stream));
+  if (ntask > 0) {
+    LAPY_CUDA_TRY(cudaMemcpyAsync(d_tseg, task_seg.data(), 4 * (size_t)ntask, cudaMemcpyHostToDevice, stream));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(d_tg0, task_g0.data(), 4 * (size_t)ntask, cudaMemcpyHostToDevice, stream));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(d_tg1, task_g1.data(), 4 * (size_t)ntask, cudaMemcpyHostToDevice, stream));
+  }
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_vct, vc_task.data(), 4 * vc_task.size(), cudaMemcpyHostToDevice, stream));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(d_offp, off_pad.data(), 8 * off_pad.size(), cudaMemcpyHostToDevice, stream));
   if (off[nseg] > 0) LAPY_CUDA_TRY(cudaMemsetAsync(d_kc, 0, 8 * (size_t)off[nseg], stream));
   LAPY_CUDA_TRY(cudaMemsetAsync(d_fail, 0, 4 * (size_t)nseg, stream));
   if (nagg > 0) {
     coarse_galerkin_kernel<<<lapy_ceil_div(nagg, 128), 128, 0, stream>>>(nagg, d_agg, d_ptr, d_row, d_sid, d_seg, d_off,
                                                                          indptr, indices, k64, d_kc);
     LAPY_TRY(lapy_check_launch("coarse_galerkin_kernel"));
-    coarse_inverse_kernel<<<nseg, kInvThreads, 0, stream>>>(d_seg, d_off, d_kc, d_kinv, d_fail);
+    coarse_inverse_kernel<<<nseg, kInvThreads, 0, stream>>>(d_seg, d_off, d_offp, d_kc, d_full, d_kinv, d_kvec,
+                                                            d_kscale, d_fail);
     LAPY_TRY(lapy_check_launch("coarse_inverse_kernel"));
   }
   // the host vectors are pageable: the copies complete before they go away
@@ -377,8 +488,15 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   pc->agg_row = d_row;
   pc->agg_sid = d_sid;
   pc->seg_agg = d_seg;
-  pc->kinv_off = d_off;
+  pc->kinv_off = d_offp;
   pc->kinv = d_kinv;
+  pc->kvec = d_kvec;
+  pc->kscale = d_kscale;
+  pc->ntask = ntask;
+  pc->task_seg = d_tseg;
+  pc->task_g0 = d_tg0;
+  pc->task_g1 = d_tg1;
+  pc->vc_task = d_vct;
   pc->nvc = nvc;
   pc->naslot = seg_aslot[nseg];
   pc->max_seg_agg = nseg > 0 ? *std::max_element(nc.begin(), nc.end()) : 0;

@@ -32,6 +32,11 @@ constexpr int kPlanCtasPerSm = 5; // resident CTAs per SM the warp plan assumes 
 // more pieces, or coarse unknowns, than these.
 constexpr int kFoldPieces = 64;
 constexpr int kFoldAggs = 1024;
+// Coarse rows a warp computes together in the coarse solve (each staged
+// residual value read from shared memory serves that many rows).
+#ifndef LAPY_COARSE_RW
+#define LAPY_COARSE_RW 2
+#endif
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -543,40 +548,179 @@ __device__ __forceinline__ void coarse_restrict(const PcgArgs<V>& a, const int32
   })
 }
 
-// Two-level preconditioner, coarse solve: yc = (W'KW)^-1 rc per segment (one
-// warp per coarse row) and csl = rc .* yc.
-template <typename V, int NP>
-__device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t* st, bool all) {
-  using S = ScalarOf<V>;
+// BF16 element e (0..3) of four packed in a uint2 (element 0 in the low half
+// of .x): a BF16 value is the upper 16 bits of the FP32 with the same value.
+__device__ __forceinline__ float bf16x4_elem(const uint2& w, int e) {
+  const unsigned word = (e < 2) ? w.x : w.y;
+  return __uint_as_float((e & 1) ? (word & 0xffff0000u) : (word << 16));
+}
+
+// Rows of the coarse product for one warp: acc[r][q] += sum_j R[r][j] x[j][q]
+// over j < jend (a multiple of 4), for the nr <= RW rows starting at kr (row
+// stride ld, a multiple of 8).  Lane l streams entries 4l .. 4l+3 of every
+// 128, one 8-byte load per row, the next group's loads issued before the
+// current group is used (two groups of RW loads in flight per lane); each x
+// value read serves RW rows.  SWZ: x is the staged copy in shared memory,
+// entry j at (j % 4) * (ld / 4) + j / 4, so that the 32 lanes read 32
+// consecutive entries (no bank conflicts); otherwise x is rc in global
+// memory, entry j at j.
+template <int NP, int RW, bool SWZ>
+__device__ __forceinline__ void coarse_rows(const uint16_t* __restrict__ kr, int ld, int jend, int nr,
+                                            const float* x, float (&acc)[RW][NP]) {
   const int lane = threadIdx.x & 31;
-  FOR_MY_AGGS(a, {
-    if (!all) {
-      bool act = false;
+  const int l4 = ld >> 2;
+  const uint2* __restrict__ kq = reinterpret_cast<const uint2*>(kr);  // 4 entries per uint2
+  uint2 w[RW];
 #pragma unroll
-      for (int q = 0; q < NP; ++q) act |= st[s * NP + q] == kActive;
-      if (!act) continue;
-    }
-    const int base = a.pc.seg_agg[s];
-    const int nc = a.pc.seg_agg[s + 1] - base;
-    const float* __restrict__ kr = a.pc.kinv + a.pc.kinv_off[s] + (int64_t)(g - base) * nc;
-    const S* __restrict__ rcs = a.rc + (int64_t)base * NP;
-    S acc[NP];
+  for (int r = 0; r < RW; ++r)
+    w[r] = (r < nr && 4 * lane < jend) ? __ldg(kq + r * l4 + lane) : make_uint2(0u, 0u);
+  for (int j4 = lane; 4 * j4 < jend; j4 += 32) {
+    const int jn = j4 + 32;
+    uint2 wn[RW];
 #pragma unroll
-    for (int q = 0; q < NP; ++q) acc[q] = S(0);
-    for (int j = lane; j < nc; j += 32) {
-      const S kv = (S)__ldg(kr + j);
+    for (int r = 0; r < RW; ++r) wn[r] = (r < nr && 4 * jn < jend) ? __ldg(kq + r * l4 + jn) : make_uint2(0u, 0u);
 #pragma unroll
-      for (int q = 0; q < NP; ++q) acc[q] += kv * rcs[(int64_t)j * NP + q];
-    }
+    for (int e = 0; e < 4; ++e) {
+      float xv[NP];
+      load_row<float, NP>(x, SWZ ? e * l4 + j4 : 4 * j4 + e, xv);
 #pragma unroll
-    for (int q = 0; q < NP; ++q) {
-      const S y = warp_sum(acc[q]);
-      if (lane == q) {
-        a.yc[(int64_t)g * NP + q] = y;
-        a.csl[(int64_t)g * NP + q] = y * a.rc[(int64_t)g * NP + q];
+      for (int r = 0; r < RW; ++r) {
+        const float kv = bf16x4_elem(w[r], e);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) acc[r][q] = fmaf(kv, xv[q], acc[r][q]);
       }
     }
-  })
+#pragma unroll
+    for (int r = 0; r < RW; ++r) w[r] = wn[r];
+  }
+}
+
+// Two-level preconditioner, coarse solve: yc = (W'KW)^-1 rc per segment and
+// csl = rc .* yc, with (W'KW)^-1 = c v v' + R (R in BF16).  CTA-wide tasks
+// of up to kCoarseTaskRows coarse rows of one segment: the CTA stages the
+// segment's rc (zero-padded to ld) and v'rc in shared memory when they fit
+// (`stage`, shared with the SpMM staging buffer), then every warp computes
+// RW rows at a time; otherwise each warp reads rc from global memory (only
+// below nc) and forms v'rc itself.
+template <typename V, int NP>
+__device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t* st, bool all, float* stage,
+                                             int stage_floats) {
+  static_assert(sizeof(V) == 4, "the two-level preconditioner runs FP32 iterations");
+  constexpr int RW = (NP <= 4) ? LAPY_COARSE_RW : 1;  // rows per warp pass (48-register budget)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ float s_vrc[NP];
+  __shared__ float s_red[kWarps][NP];
+  int staged = -1;
+  for (int vc = blockIdx.x; vc < a.pc.nvc; vc += gridDim.x) {
+    for (int t = a.pc.vc_task[vc]; t < a.pc.vc_task[vc + 1]; ++t) {
+      const int s = a.pc.task_seg[t];
+      if (!all) {
+        bool act = false;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) act |= st[s * NP + q] == kActive;
+        if (!act) continue;  // the same decision in every thread of the CTA
+      }
+      const int base = a.pc.seg_agg[s];
+      const int nc = a.pc.seg_agg[s + 1] - base;
+      const int ld = (nc + 7) & ~7;
+      const float* __restrict__ rcs = a.rc + (int64_t)base * NP;
+      const float* __restrict__ vs = a.pc.kvec + base;
+      const bool use_stage = ld * NP <= stage_floats;
+      float vrc[NP];
+      if (use_stage) {
+        if (s != staged) {
+          __syncthreads();  // every warp is done with the previous segment
+          float part[NP];
+#pragma unroll
+          for (int q = 0; q < NP; ++q) part[q] = 0.f;
+          const int l4 = ld >> 2;
+          for (int j = threadIdx.x; j < ld; j += blockDim.x) {
+            float xv[NP];
+            if (j < nc) {
+              load_row<float, NP>(rcs, j, xv);
+              const float vj = vs[j];
+#pragma unroll
+              for (int q = 0; q < NP; ++q) part[q] = fmaf(vj, xv[q], part[q]);
+            } else {
+#pragma unroll
+              for (int q = 0; q < NP; ++q) xv[q] = 0.f;
+            }
+            store_row<float, NP>(stage, (j & 3) * l4 + (j >> 2), xv);
+          }
+#pragma unroll
+          for (int q = 0; q < NP; ++q) {
+            const float w = warp_sum(part[q]);
+            if (lane == 0) s_red[warp][q] = w;
+          }
+          __syncthreads();
+          if (threadIdx.x < NP) {
+            float tot = 0.f;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) tot += s_red[w][threadIdx.x];
+            s_vrc[threadIdx.x] = tot;
+          }
+          __syncthreads();
+          staged = s;
+        }
+#pragma unroll
+        for (int q = 0; q < NP; ++q) vrc[q] = s_vrc[q];
+      } else {
+        float part[NP];
+#pragma unroll
+        for (int q = 0; q < NP; ++q) part[q] = 0.f;
+        for (int j = lane; j < nc; j += 32) {
+          float xv[NP];
+          load_row<float, NP>(rcs, j, xv);
+          const float vj = vs[j];
+#pragma unroll
+          for (int q = 0; q < NP; ++q) part[q] = fmaf(vj, xv[q], part[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < NP; ++q) vrc[q] = warp_sum(part[q]);
+      }
+      const int g0 = a.pc.task_g0[t], g1 = a.pc.task_g1[t];
+      const float c = a.pc.kscale[s];
+      for (int r0 = g0 + warp * RW; r0 < g1; r0 += kWarps * RW) {
+        const int nr = min(RW, g1 - r0);
+        const uint16_t* kr = a.pc.kinv + a.pc.kinv_off[s] + (int64_t)(r0 - base) * ld;
+        float acc[RW][NP];
+#pragma unroll
+        for (int r = 0; r < RW; ++r)
+#pragma unroll
+          for (int q = 0; q < NP; ++q) acc[r][q] = 0.f;
+        if (use_stage) {
+          coarse_rows<NP, RW, true>(kr, ld, ld, nr, stage, acc);
+        } else {
+          // rc is read only below nc (what follows may be another segment's)
+          const int body = nc & ~3;
+          coarse_rows<NP, RW, false>(kr, ld, body, nr, rcs, acc);
+          for (int j = body + lane; j < nc; j += 32) {
+            float xv[NP];
+            load_row<float, NP>(rcs, j, xv);
+#pragma unroll
+            for (int r = 0; r < RW; ++r) {
+              const float kv = (r < nr) ? __uint_as_float((unsigned)kr[r * ld + j] << 16) : 0.f;
+#pragma unroll
+              for (int q = 0; q < NP; ++q) acc[r][q] = fmaf(kv, xv[q], acc[r][q]);
+            }
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < RW; ++r) {
+          const int g = r0 + r;
+          const float cv = (r < nr) ? c * vs[g - base] : 0.f;
+#pragma unroll
+          for (int q = 0; q < NP; ++q) {
+            const float y = warp_sum(acc[r][q]) + cv * vrc[q];
+            if (r < nr && lane == r * NP + q) {
+              a.yc[(int64_t)g * NP + q] = y;
+              a.csl[(int64_t)g * NP + q] = y * a.rc[(int64_t)g * NP + q];
+            }
+          }
+        }
+      }
+    }
+  }
   if (a.fold) {
     __syncthreads();
     fold_aggs<V, NP>(a, a.csl, a.aslot);
@@ -661,8 +805,12 @@ __device__ __forceinline__ void factor_first_half(const PcgArgs<V>& a, int u0, i
 template <typename V, int NP, int PC, bool RU>
 __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArgs<V> a) {
   using S = ScalarOf<V>;
-  __shared__ V sval_all[kWarps * kStageWarp];
-  __shared__ int32_t sidx_all[kWarps * kStageWarp];
+  // one buffer: the SpMM's staged slices (values, then column indices) or,
+  // in the coarse phase, a segment's restricted residual
+  constexpr int kStageBytes = kWarps * kStageWarp * (int)(sizeof(V) + sizeof(int32_t));
+  __shared__ __align__(16) unsigned char stage_raw[kStageBytes];
+  V* sval_all = reinterpret_cast<V*>(stage_raw);
+  int32_t* sidx_all = reinterpret_cast<int32_t*>(stage_raw + kWarps * kStageWarp * sizeof(V));
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gw = blockIdx.x * kWarps + warp, nw = gridDim.x * kWarps;
   V* wval = sval_all + warp * kStageWarp;
@@ -738,7 +886,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     if (!grid_sync(a.bar)) return;
     coarse_restrict<V, NP>(a, nullptr, true);
     if (!grid_sync(a.bar)) return;
-    coarse_solve<V, NP>(a, nullptr, true);
+    coarse_solve<V, NP>(a, nullptr, true, reinterpret_cast<float*>(stage_raw), kStageBytes / 4);
   }
   if constexpr (PC == kPrecFactored) {  // r'z = ||G r||^2; P = G'(G r) below
     if (!grid_sync(a.bar)) return;
@@ -1028,7 +1176,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       coarse_restrict<V, NP>(a, st_cur, false);
       if (!grid_sync(a.bar)) return;
       mark(3);
-      coarse_solve<V, NP>(a, st_cur, false);
+      coarse_solve<V, NP>(a, st_cur, false, reinterpret_cast<float*>(stage_raw), kStageBytes / 4);
       if (!grid_sync(a.bar)) return;
       mark(4);
     }

@@ -52,6 +52,9 @@ int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream);
 
 enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1, kPrecTwoLevel = 2 };
 
+// Coarse rows per coarse-solve task: 8 warps x 4 rows.
+constexpr int kCoarseTaskRows = 32;
+
 // Sliced-ELL copy of a CSR matrix: one slice per 32-row unit of a chunk
 // table, entries stored slot-major inside a slice (element k of the slice's
 // row `lane` at slice_ptr[u] + 32 k + lane), rows padded to the slice's
@@ -95,8 +98,23 @@ struct PcgPrecondDesc {
   const int32_t* agg_row = nullptr;   //   (CSR, rows ascending)
   const int32_t* agg_sid = nullptr;   // nagg: segment of each aggregate
   const int32_t* seg_agg = nullptr;   // nseg + 1: aggregate range of each segment
-  const int64_t* kinv_off = nullptr;  // nseg: offset of the segment's nc x nc inverse
-  const float* kinv = nullptr;        // dense (W'KW)^-1 blocks, row-major, FP32
+  // (W'KW)^-1 of segment s = kscale[s] v v' + R, v = kvec[seg_agg[s] ..] the
+  // unit eigenvector of the smallest eigenvalue of W'KW (FP32) and R the
+  // remainder, stored in BF16 (row-major, rows padded to ld = nc rounded up
+  // to 8, pad entries zero): with the dominant mode of the inverse kept
+  // apart, 16-bit storage of the rest leaves the preconditioner SPD
+  const int64_t* kinv_off = nullptr;  // nseg: offset of the segment's nc x ld remainder
+  const uint16_t* kinv = nullptr;     // BF16 remainders
+  const float* kvec = nullptr;        // nagg: v, per segment
+  const float* kscale = nullptr;      // nseg: c = v' (W'KW)^-1 v
+  // coarse-solve tasks: coarse rows [task_g0[t], task_g1[t]) (global
+  // indices, at most kCoarseTaskRows, one segment); virtual CTA v runs tasks
+  // [vc_task[v], vc_task[v+1]), contiguous and of about equal cost
+  int ntask = 0;
+  const int32_t* task_seg = nullptr;  // ntask
+  const int32_t* task_g0 = nullptr;   // ntask
+  const int32_t* task_g1 = nullptr;   // ntask
+  const int32_t* vc_task = nullptr;   // nvc + 1
   // coarse work split over the PCG's virtual CTAs: aggregates
   // [vc_agg[v], vc_agg[v+1]) (contiguous, about equal cost) go to virtual
   // CTA v; segment s owns the reduction slots [seg_aslot[s], seg_aslot[s+1])

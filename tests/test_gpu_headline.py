@@ -65,7 +65,9 @@ def _with_degenerate_triangles(mesh, count, scale):
 
 def test_batched_clamp_is_per_mesh(cuda_ok):
     """Degenerate elements of each mesh get that mesh's own clamp: the batch's
-    blocks equal single-mesh assembly bit for bit."""
+    blocks equal single-mesh assembly to the last bits of the mean measure,
+    which the two paths sum in different orders (the clamp enters both the
+    mass and the cotangent terms of the degenerate elements)."""
     from lapy_gb300 import Solver, meshes, shapedna
 
     ms = [_with_degenerate_triangles(meshes.icosphere(2), 3, 1.0),
@@ -80,8 +82,8 @@ def test_batched_clamp_is_per_mesh(cuda_ok):
         A1, M1 = single.stiffness, single.mass
         r0, r1 = fem.seg_row[i], fem.seg_row[i + 1]
         k0, k1 = indptr[r0], indptr[r1]
-        np.testing.assert_array_equal(a[k0:k1], sparse.csr_matrix(A1).data)
-        np.testing.assert_array_equal(m[k0:k1], sparse.csr_matrix(M1).data)
+        np.testing.assert_allclose(a[k0:k1], sparse.csr_matrix(A1).data, rtol=1e-14, atol=0)
+        np.testing.assert_allclose(m[k0:k1], sparse.csr_matrix(M1).data, rtol=1e-14, atol=0)
         # the mass carries this mesh's clamp (the oracle's mean is NumPy's)
         Mref = oracle.assemble_sorted(np.asarray(mesh.v), np.asarray(mesh.t))[1]
         np.testing.assert_allclose(m[k0:k1], Mref.data, rtol=1e-14, atol=0)
