@@ -378,11 +378,15 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   }
 
   // coarse-solve tasks (up to kCoarseTaskRows coarse rows of one segment),
-  // split over the virtual CTAs in contiguous ranges of about equal cost (the
-  // BF16 entries they stream, plus a fixed cost per row and per task); the
-  // aggregates of a virtual CTA's tasks are also its share of the
-  // restriction, and the reduction slots of each segment's coarse partial
-  // sums follow from that split
+  // split over the virtual CTAs in contiguous ranges of about equal time.  A
+  // task's time (ns) is modelled as a fixed part (staging the segment's
+  // residual, three CTA barriers), a memory round trip per warp pass (each
+  // warp computes kCoarseRowsPerPass rows per pass) plus the 128-entry row
+  // groups it streams, and its BF16 bytes at a CTA's share of the HBM
+  // bandwidth; small segments are dominated by the fixed parts, which a
+  // byte count alone would miss.  The aggregates of a virtual CTA's tasks
+  // are also its share of the restriction, and the reduction slots of each
+  // segment's coarse partial sums follow from that split.
   std::vector<int32_t> task_seg, task_g0, task_g1;
   std::vector<double> task_cost;
   for (int s = 0; s < nseg; ++s)
@@ -391,7 +395,12 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
       task_seg.push_back(s);
       task_g0.push_back(g);
       task_g1.push_back(g1);
-      task_cost.push_back((double)(g1 - g) * (double)(pad8(nc[s]) + 64) + 512.0);
+      const int rows = g1 - g;
+      const double passes = (double)((rows + kWarpsPerCta * kCoarseRowsPerPass - 1) /
+                                     (kWarpsPerCta * kCoarseRowsPerPass));
+      const double groups = (double)((pad8(nc[s]) + 127) / 128);
+      task_cost.push_back(1200.0 + passes * (800.0 + 250.0 * groups) +
+                          2.0 * rows * (double)pad8(nc[s]) / 8.7);
     }
   const int ntask = (int)task_seg.size();
   std::vector<int32_t> vc_task(nvc + 1, 0);

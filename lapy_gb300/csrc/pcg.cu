@@ -27,16 +27,13 @@ constexpr int kPcgThreads = 256;
 constexpr int kWarps = kPcgThreads / 32;
 constexpr int kUnit = 32;
 constexpr int kStageWarp = 384;   // staged nonzeros per warp (values + column indices)
+constexpr int kSellShort = 8;     // SELL slices up to this width take the all-loads-first path
 constexpr int kPlanCtasPerSm = 5; // resident CTAs per SM the warp plan assumes (48 registers)
 // Partial sums are folded into per-CTA reduction slots when a segment has
 // more pieces, or coarse unknowns, than these.
 constexpr int kFoldPieces = 64;
 constexpr int kFoldAggs = 1024;
-// Coarse rows a warp computes together in the coarse solve (each staged
-// residual value read from shared memory serves that many rows).
-#ifndef LAPY_COARSE_RW
-#define LAPY_COARSE_RW 2
-#endif
+
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -410,14 +407,36 @@ __device__ __forceinline__ void sell_unit_spmm(const SellMatrix<V>& M, const V* 
   V acc[NP];
 #pragma unroll
   for (int q = 0; q < NP; ++q) acc[q] = V(0);
-#pragma unroll 4
-  for (int k = 0; k < w; ++k) {
-    const V a = __ldg(vp + 32 * k);
-    const int32_t c = __ldg(cp + 32 * k);
-    V xr[NP];
-    load_row<V, NP>(Xin, c, xr);
+  if (w <= kSellShort) {
+    // short slices (mesh rows: up to 7 entries): every value and column
+    // index of the slice is requested at once, then every gather, so the
+    // unit costs two dependent memory round trips
+    V av[kSellShort];
+    int32_t cv[kSellShort];
 #pragma unroll
-    for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
+    for (int k = 0; k < kSellShort; ++k) {
+      av[k] = (k < w) ? __ldg(vp + 32 * k) : V(0);
+      cv[k] = (k < w) ? __ldg(cp + 32 * k) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kSellShort; ++k) {
+      if (k < w) {
+        V xr[NP];
+        load_row<V, NP>(Xin, cv[k], xr);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) acc[q] += av[k] * xr[q];
+      }
+    }
+  } else {
+#pragma unroll 4
+    for (int k = 0; k < w; ++k) {
+      const V a = __ldg(vp + 32 * k);
+      const int32_t c = __ldg(cp + 32 * k);
+      V xr[NP];
+      load_row<V, NP>(Xin, c, xr);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
+    }
   }
   const int row = ur0 + lane;
   if (row < ur1) {
@@ -606,7 +625,10 @@ template <typename V, int NP>
 __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t* st, bool all, float* stage,
                                              int stage_floats) {
   static_assert(sizeof(V) == 4, "the two-level preconditioner runs FP32 iterations");
-  constexpr int RW = (NP <= 4) ? LAPY_COARSE_RW : 1;  // rows per warp pass (48-register budget)
+  // rows per warp pass (each staged residual value read from shared memory
+  // serves that many rows; bounded by the 48-register budget)
+  constexpr int RW = (NP <= 4) ? kCoarseRowsPerPass : 1;
+  static_assert(kWarps == kWarpsPerCta, "coarse task plan and kernel disagree on the CTA size");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __shared__ float s_vrc[NP];
   __shared__ float s_red[kWarps][NP];

@@ -52,8 +52,14 @@ int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream);
 
 enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1, kPrecTwoLevel = 2 };
 
-// Coarse rows per coarse-solve task: 8 warps x 4 rows.
+// Coarse rows per coarse-solve task: 8 warps x 4 rows; a warp computes
+// kCoarseRowsPerPass of them at a time (block widths up to 4).
 constexpr int kCoarseTaskRows = 32;
+constexpr int kWarpsPerCta = 8;
+#ifndef LAPY_COARSE_RW
+#define LAPY_COARSE_RW 2
+#endif
+constexpr int kCoarseRowsPerPass = LAPY_COARSE_RW;
 
 // Sliced-ELL copy of a CSR matrix: one slice per 32-row unit of a chunk
 // table, entries stored slot-major inside a slice (element k of the slice's
