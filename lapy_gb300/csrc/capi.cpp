@@ -51,17 +51,25 @@ static double g_prof[kProfSlots] = {0};
 void lapy_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 bool lapy_profile_enabled() { return g_prof_on; }
 
-void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int eb) {
+void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int eb, int precond,
+                          double coarse_bytes) {
   std::lock_guard<std::mutex> lock(g_prof_mu);
   g_prof[0] += ms;
   g_prof[1] += 1;
   g_prof[2] += (double)iters;
   g_prof[3] += (double)rows;
   g_prof[4] += (double)nnz;
-  // algorithmic bytes of the fused Jacobi-PCG iteration over the rows it
-  // touched: matrix (value + column index per nonzero, row pointer per row),
-  // 11 vector streams of p values and 2 of the Jacobi diagonal
-  g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (4 + 11.0 * p * eb + 2.0 * eb);
+  // algorithmic bytes of the PCG iterations over the rows they touched:
+  // matrix (value + column index per nonzero); Jacobi: a row pointer per
+  // row, 11 vector streams of p values and 2 of the Jacobi diagonal;
+  // two-level (precond 2): 12 vector streams (SpMM: P in, Q out; update: X,
+  // P, Q, R in, X, R out; restriction: R in; direction: R, P in, P out), 2 of
+  // the diagonal, the aggregate index per row, and the BF16 coarse inverse
+  // the coarse solves streamed
+  if (precond == 2)
+    g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (12.0 * p * eb + 2.0 * eb + 4.0) + coarse_bytes;
+  else
+    g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (4 + 11.0 * p * eb + 2.0 * eb);
 }
 
 void lapy_profile_add_phases(const double* ms) {

@@ -328,23 +328,105 @@ __global__ void __launch_bounds__(kInvThreads) coarse_inverse_kernel(const int32
   }
 }
 
+static int host_threads(int nseg) {
+  return std::max(1, std::min<int>(nseg, std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+}
+
+int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, const int32_t* seg_row, int nseg,
+                         int32_t* perm, int32_t* lab_new) {
+  std::vector<int32_t> lab(n, -1);
+  const int nthr = host_threads(nseg);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nthr; ++t)
+    pool.emplace_back([&, t]() {
+      std::vector<int32_t> order, first, cnt, fill, agg_order, agg_rank, queue;
+      for (int s = t; s < nseg; s += nthr) {
+        const int32_t r0 = seg_row[s], r1 = seg_row[s + 1];
+        const int nc = aggregate_segment(r0, r1, hptr, hidx, lab.data());
+        if (nc <= 0) {  // no coarse space: rows keep their order, no aggregate
+          for (int32_t v = r0; v < r1; ++v) {
+            perm[v] = v;
+            lab_new[v] = -1;
+          }
+          continue;
+        }
+        // aggregates in breadth-first order over the aggregate graph (from
+        // the aggregate of the segment's first row; neighbours in the order
+        // their member rows and CSR entries are met), so that neighbouring
+        // aggregates get nearby numbers
+        cnt.assign(nc + 1, 0);
+        for (int32_t v = r0; v < r1; ++v) ++cnt[lab[v] + 1];
+        for (int g = 0; g < nc; ++g) cnt[g + 1] += cnt[g];
+        order.resize(r1 - r0);
+        fill.assign(cnt.begin(), cnt.end() - 1);
+        for (int32_t v = r0; v < r1; ++v) order[fill[lab[v]]++] = v;  // members, rows ascending
+        agg_rank.assign(nc, -1);
+        agg_order.clear();
+        for (int seed = 0; seed < nc; ++seed) {
+          if (agg_rank[seed] >= 0) continue;
+          agg_rank[seed] = (int32_t)agg_order.size();
+          agg_order.push_back(seed);
+          for (size_t qi = agg_order.size() - 1; qi < agg_order.size(); ++qi) {
+            const int g = agg_order[qi];
+            for (int32_t m = cnt[g]; m < cnt[g + 1]; ++m) {
+              const int32_t u = order[m];
+              for (int32_t k = hptr[u]; k < hptr[u + 1]; ++k) {
+                const int32_t w = hidx[k];
+                if (w < r0 || w >= r1) continue;
+                const int32_t h = lab[w];
+                if (h >= 0 && agg_rank[h] < 0) {
+                  agg_rank[h] = (int32_t)agg_order.size();
+                  agg_order.push_back(h);
+                }
+              }
+            }
+          }
+        }
+        int32_t pos = r0;
+        for (int i = 0; i < nc; ++i) {
+          const int g = agg_order[i];
+          for (int32_t m = cnt[g]; m < cnt[g + 1]; ++m) {
+            perm[pos] = order[m];
+            lab_new[pos] = i;
+            ++pos;
+          }
+        }
+      }
+    });
+  for (auto& th : pool) th.join();
+  return LAPY_OK;
+}
+
 int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64,
                     const int32_t* seg_row, int nseg, int nvc, void* mem, size_t bytes,
-                    PcgPrecondDesc<float>* pc, cudaStream_t stream) {
+                    PcgPrecondDesc<float>* pc, cudaStream_t stream, const int32_t* lab_in) {
   nvc = std::max(nvc, 1);
   if (bytes < two_level_bytes(n, seg_row, nseg, nvc)) return LAPY_ERR_WORKSPACE;
-  // pattern to the host
-  std::vector<int32_t> hptr(n + 1);
-  LAPY_CUDA_TRY(cudaMemcpyAsync(hptr.data(), indptr, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, stream));
-  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
-  const int64_t nnz = hptr[n];
-  std::vector<int32_t> hidx(nnz);
-  LAPY_CUDA_TRY(cudaMemcpyAsync(hidx.data(), indices, 4 * (size_t)nnz, cudaMemcpyDeviceToHost, stream));
-  LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
-
   std::vector<int32_t> lab(n, -1), nc(nseg, 0);
-  const int nthr = std::max(1, std::min<int>(nseg, std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
-  {
+  bool contiguous = false;
+  if (lab_in) {
+    // labels given (local aggregate ids, rows of an aggregate contiguous and
+    // aggregates numbered in row order)
+    std::copy(lab_in, lab_in + n, lab.begin());
+    contiguous = true;
+    for (int s = 0; s < nseg; ++s) {
+      int32_t mx = -1;
+      for (int32_t v = seg_row[s]; v < seg_row[s + 1]; ++v) {
+        if (lab[v] < mx || lab[v] > mx + 1) contiguous = false;
+        mx = std::max(mx, lab[v]);
+      }
+      nc[s] = mx + 1;
+    }
+  } else {
+    // pattern to the host, aggregation there
+    std::vector<int32_t> hptr(n + 1);
+    LAPY_CUDA_TRY(cudaMemcpyAsync(hptr.data(), indptr, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, stream));
+    LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+    const int64_t nnz = hptr[n];
+    std::vector<int32_t> hidx(nnz);
+    LAPY_CUDA_TRY(cudaMemcpyAsync(hidx.data(), indices, 4 * (size_t)nnz, cudaMemcpyDeviceToHost, stream));
+    LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+    const int nthr = host_threads(nseg);
     std::vector<std::thread> pool;
     for (int t = 0; t < nthr; ++t)
       pool.emplace_back([&, t]() {
@@ -497,6 +579,7 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   pc->agg_row = d_row;
   pc->agg_sid = d_sid;
   pc->seg_agg = d_seg;
+  pc->agg_contig = contiguous ? 1 : 0;
   pc->kinv_off = d_offp;
   pc->kinv = d_kinv;
   pc->kvec = d_kvec;

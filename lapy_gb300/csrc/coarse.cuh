@@ -26,8 +26,21 @@ size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg, int nvc);
 // its dense inverse (FP64 Cholesky, stored FP32) on the device, and the
 // split of the coarse work over the nvc virtual CTAs of the PCG's warp plan.
 // Fills the two-level fields of `pc` (which keeps its Jacobi diagonal).
+// `lab_in` (host, may be null): aggregate labels already planned
+// (plan_aggregate_order), used instead of aggregating here.
 int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64,
                     const int32_t* seg_row, int nseg, int nvc, void* mem, size_t bytes,
-                    PcgPrecondDesc<float>* pc, cudaStream_t stream);
+                    PcgPrecondDesc<float>* pc, cudaStream_t stream, const int32_t* lab_in = nullptr);
+
+// Row order of a batch (host, pattern on the host) that makes every
+// aggregate a contiguous row range: each segment is aggregated as
+// build_two_level does, its aggregates are ordered breadth-first over the
+// aggregate graph, and the rows of an aggregate keep their relative order.
+// perm[new] = old (rows stay in their segment); lab_new[new] = local
+// aggregate id in the new order (-1 for segments without a coarse space,
+// whose rows keep their order).  Neighbouring rows thereby sit in the same
+// or nearby aggregates, so the gathers of a sparse product stay close.
+int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, const int32_t* seg_row, int nseg,
+                         int32_t* perm, int32_t* lab_new);
 
 }  // namespace lapy

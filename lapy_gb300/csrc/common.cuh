@@ -28,7 +28,8 @@ void lapy_set_last_message(const char* fmt, ...);
 void lapy_count_launch();
 // PCG profile accumulation (enabled by lapy_profile_enable).
 bool lapy_profile_enabled();
-void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int elem_bytes);
+void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int elem_bytes,
+                          int precond, double coarse_bytes);
 void lapy_profile_add_reorth(long long steps, long long second_passes);
 // Per-phase device time of the persistent PCG (profile mode): the interval
 // between consecutive grid-barrier exits, accumulated per phase: initialisation,

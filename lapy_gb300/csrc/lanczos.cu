@@ -648,6 +648,53 @@ __global__ void rr_finish_kernel(int keff, int k, const double* __restrict__ Lm,
   }
 }
 
+// ---- aggregate-contiguous row order (two-level eigensolves) ---------------
+// New row i is old row perm[i]; its entries are those of the old row with
+// columns renumbered by iperm and sorted ascending (insertion sort on the
+// row's own output range); pos[k] = old position of new entry k.
+__global__ void permute_pattern_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                                       const int32_t* __restrict__ indices, const int32_t* __restrict__ perm,
+                                       const int32_t* __restrict__ iperm, const int32_t* __restrict__ pindptr,
+                                       int32_t* __restrict__ pindices, int32_t* __restrict__ pos) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t o = perm[i];
+  const int32_t kb = indptr[o], len = indptr[o + 1] - kb, out = pindptr[i];
+  for (int32_t t = 0; t < len; ++t) {
+    const int32_t c = iperm[indices[kb + t]], k = kb + t;
+    int32_t j = t;
+    while (j > 0 && pindices[out + j - 1] > c) {
+      pindices[out + j] = pindices[out + j - 1];
+      pos[out + j] = pos[out + j - 1];
+      --j;
+    }
+    pindices[out + j] = c;
+    pos[out + j] = k;
+  }
+}
+
+__global__ void inverse_perm_kernel(int64_t n, const int32_t* __restrict__ perm, int32_t* __restrict__ iperm) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) iperm[perm[i]] = (int32_t)i;
+}
+
+// out[k] = in[idx[k]]
+__global__ void gather_f64_kernel(int64_t m, const int32_t* __restrict__ idx, const double* __restrict__ in,
+                                  double* __restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < m) out[k] = in[idx[k]];
+}
+
+// Rows back to the caller's order: out[perm[i]][c] = in[i][c] (ncol columns).
+__global__ void unpermute_rows_kernel(int64_t n, int ncol, const int32_t* __restrict__ perm,
+                                      const double* __restrict__ in, double* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * ncol) return;
+  const int64_t i = t / ncol;
+  const int c = (int)(t - i * ncol);
+  out[(int64_t)perm[i] * ncol + c] = in[t];
+}
+
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
@@ -676,6 +723,8 @@ struct EigPtrs {
   double* Ak; double* Mk; double* Cneg; double* theta2; double* V; double* eigw2;
   int32_t* active; int32_t* nsize; int32_t* fail; int32_t* nconv; double* resid;
   double* wn0; double* wn1; int32_t* active2; unsigned long long* rcnt;
+  // aggregate-contiguous copy of the system (two-level only)
+  int32_t* perm; int32_t* iperm; int32_t* pindptr; int32_t* pindices; int32_t* ppos; double* pa; double* pm;
 };
 
 static void plan_eig(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, int k, int p, int max_vectors,
@@ -759,6 +808,14 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.wn1 = (double*)take(8 * (size_t)ns * p);
   e.active2 = (int32_t*)take(4 * ns);
   e.rcnt = (unsigned long long*)take(16);
+  const bool reorder = P.precond == kPrecTwoLevel;
+  e.perm = (int32_t*)take(reorder ? 4 * n : 0);
+  e.iperm = (int32_t*)take(reorder ? 4 * n : 0);
+  e.pindptr = (int32_t*)take(reorder ? 4 * (n + 1) : 0);
+  e.pindices = (int32_t*)take(reorder ? 4 * nnz : 0);
+  e.ppos = (int32_t*)take(reorder ? 4 * nnz : 0);
+  e.pa = (double*)take(reorder ? 8 * nnz : 0);
+  e.pm = (double*)take(reorder ? 8 * std::max<int64_t>(nnz, n) : 0);
   if (q) *q = e;
   return off + 256;
 }
@@ -917,6 +974,46 @@ struct EigResult {
   int blocks = 0;
 };
 
+// Two-level eigensolves run on an aggregate-contiguous row order of the
+// system (plan_aggregate_order): the copies (pattern, A, M) go to the
+// workspace, *indptr etc. are redirected to them, and lab_out receives the
+// aggregate labels in that order.
+static int reorder_system(const EigPlan& P, const EigPtrs& e, const int32_t** indptr, const int32_t** indices,
+                          const double** a_vals, const double** m_vals, int m_is_diag, std::vector<int32_t>* lab_out,
+                          cudaStream_t st) {
+  const int64_t n = P.n, nnz = P.nnz;
+  std::vector<int32_t> hptr(n + 1), hidx(nnz);
+  LAPY_CUDA_TRY(cudaMemcpyAsync(hptr.data(), *indptr, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, st));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(hidx.data(), *indices, 4 * (size_t)nnz, cudaMemcpyDeviceToHost, st));
+  LAPY_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<int32_t> perm(n), nptr(n + 1, 0);
+  lab_out->assign(n, -1);
+  LAPY_TRY(plan_aggregate_order(n, hptr.data(), hidx.data(), P.ct.h_seg_row.data(), P.nseg, perm.data(),
+                                lab_out->data()));
+  for (int64_t i = 0; i < n; ++i) nptr[i + 1] = nptr[i] + (hptr[perm[i] + 1] - hptr[perm[i]]);
+  LAPY_CUDA_TRY(cudaMemcpyAsync(e.perm, perm.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, st));
+  LAPY_CUDA_TRY(cudaMemcpyAsync(e.pindptr, nptr.data(), 4 * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
+  const unsigned nb = lapy_ceil_div(n, 256), zb = lapy_ceil_div(nnz, 256);
+  inverse_perm_kernel<<<nb, 256, 0, st>>>(n, e.perm, e.iperm);
+  LAPY_TRY(lapy_check_launch("inverse_perm_kernel"));
+  permute_pattern_kernel<<<nb, 256, 0, st>>>(n, *indptr, *indices, e.perm, e.iperm, e.pindptr, e.pindices, e.ppos);
+  LAPY_TRY(lapy_check_launch("permute_pattern_kernel"));
+  gather_f64_kernel<<<zb, 256, 0, st>>>(nnz, e.ppos, *a_vals, e.pa);
+  LAPY_TRY(lapy_check_launch("gather_f64_kernel"));
+  if (m_is_diag)
+    gather_f64_kernel<<<nb, 256, 0, st>>>(n, e.perm, *m_vals, e.pm);
+  else
+    gather_f64_kernel<<<zb, 256, 0, st>>>(nnz, e.ppos, *m_vals, e.pm);
+  LAPY_TRY(lapy_check_launch("gather_f64_kernel"));
+  // the host vectors are pageable: the copies complete before they go away
+  LAPY_CUDA_TRY(cudaStreamSynchronize(st));
+  *indptr = e.pindptr;
+  *indices = e.pindices;
+  *a_vals = e.pa;
+  *m_vals = e.pm;
+  return LAPY_OK;
+}
+
 static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, const int32_t* indices,
                     const double* a_vals, const double* m_vals, int m_is_diag, double sigma, double tol,
                     double inner_rtol, double round_rtol, int inner_maxiter, uint64_t seed, double* evals,
@@ -924,6 +1021,9 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   const int64_t n = P.n;
   const int p = P.p, ns = P.nseg, keff = P.keff, lda = P.lda, k = P.k;
   const int G = spmm_pick_group(n, P.nnz);
+  const bool reorder = P.precond == kPrecTwoLevel;
+  std::vector<int32_t> lab;
+  if (reorder) LAPY_TRY(reorder_system(P, e, &indptr, &indices, &a_vals, &m_vals, m_is_diag, &lab, st));
   EigOps ops{P, e, indptr, indices, a_vals, m_vals, m_is_diag, G, st, SellMatrix<double>()};
   ChunkTable ct = P.ct, gt = P.gt;
   LAPY_TRY(upload_chunk_table(&ct, e.ct_mem, st));
@@ -961,7 +1061,7 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   }
   if (P.precond == kPrecTwoLevel)
     LAPY_TRY(build_two_level(n, indptr, indices, e.k64, P.ct.h_seg_row.data(), ns, P.ct.nvc, e.tl_mem,
-                                    e.tl_bytes, &K.pc32, st));
+                             e.tl_bytes, &K.pc32, st, reorder ? lab.data() : nullptr));
 
   LAPY_CUDA_TRY(cudaMemsetAsync(e.rcnt, 0, 16, st));
   std::vector<int32_t> hact(ns, 1), hnsize(ns, 0);
@@ -1140,7 +1240,13 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   rr_finish_kernel<<<ns, 128, 0, st>>>(keff, k, e.Mk, e.V, e.theta2, evals);
   LAPY_TRY(lapy_check_launch("rr_finish_kernel"));
   BMat X2{e.X, keff, 0};
-  LAPY_TRY(ops.gemm_nn(X2, keff, e.V, (int64_t)keff * k, k, evecs, k, k, 1.0, 0.0, nullptr));
+  if (reorder) {  // eigenvectors in the system's order, then back to the caller's (AX is free here)
+    LAPY_TRY(ops.gemm_nn(X2, keff, e.V, (int64_t)keff * k, k, e.AX, k, k, 1.0, 0.0, nullptr));
+    unpermute_rows_kernel<<<lapy_ceil_div(n * k, 256), 256, 0, st>>>(n, k, e.perm, e.AX, evecs);
+    LAPY_TRY(lapy_check_launch("unpermute_rows_kernel"));
+  } else {
+    LAPY_TRY(ops.gemm_nn(X2, keff, e.V, (int64_t)keff * k, k, evecs, k, k, 1.0, 0.0, nullptr));
+  }
   LAPY_CUDA_TRY(cudaMemcpyAsync(hfail.data(), e.fail, 4 * ns, cudaMemcpyDeviceToHost, st));
   LAPY_CUDA_TRY(cudaStreamSynchronize(st));
   for (int s = 0; s < ns; ++s)

@@ -226,6 +226,7 @@ struct PcgArgs {
   S delta2;
   int ru_every;
   unsigned long long* phase_ns;  // [kPcgPhases] device time per phase (profile mode), or null
+  unsigned long long* cwork;     // [1] BF16 bytes of the coarse inverse streamed by the coarse solves
 };
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -555,7 +556,7 @@ __device__ __forceinline__ void coarse_restrict(const PcgArgs<V>& a, const int32
     for (int q = 0; q < NP; ++q) acc[q] = S(0);
     for (int32_t m = a.pc.agg_ptr[g] + lane; m < a.pc.agg_ptr[g + 1]; m += 32) {
       V r[NP];
-      load_row<V, NP>(a.R, a.pc.agg_row[m], r);
+      load_row<V, NP>(a.R, a.pc.agg_contig ? m : a.pc.agg_row[m], r);
 #pragma unroll
       for (int q = 0; q < NP; ++q) acc[q] += (S)r[q];
     }
@@ -623,7 +624,7 @@ __device__ __forceinline__ void coarse_rows(const uint16_t* __restrict__ kr, int
 // below nc) and forms v'rc itself.
 template <typename V, int NP>
 __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t* st, bool all, float* stage,
-                                             int stage_floats) {
+                                             int stage_floats, unsigned long long& cbytes) {
   static_assert(sizeof(V) == 4, "the two-level preconditioner runs FP32 iterations");
   // rows per warp pass (each staged residual value read from shared memory
   // serves that many rows; bounded by the 48-register budget)
@@ -702,6 +703,7 @@ __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t*
       }
       const int g0 = a.pc.task_g0[t], g1 = a.pc.task_g1[t];
       const float c = a.pc.kscale[s];
+      if (threadIdx.x == 0) cbytes += 2ull * (unsigned long long)(g1 - g0) * (unsigned long long)ld;
       for (int r0 = g0 + warp * RW; r0 < g1; r0 += kWarps * RW) {
         const int nr = min(RW, g1 - r0);
         const uint16_t* kr = a.pc.kinv + a.pc.kinv_off[s] + (int64_t)(r0 - base) * ld;
@@ -849,8 +851,9 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
   __shared__ int s_act;
   __shared__ unsigned s_seen;
   if (threadIdx.x == 0) s_act = 0;
-  // rows and nonzeros this warp streamed through the SpMM phase
-  unsigned long long w_rows = 0, w_nnz = 0;
+  // rows and nonzeros this warp streamed through the SpMM phase; coarse
+  // inverse bytes this CTA streamed (thread 0)
+  unsigned long long w_rows = 0, w_nnz = 0, c_bytes = 0;
   // profile mode: thread 0 of CTA 0 adds the device time between consecutive
   // barrier exits to the phase that just ended (a barrier exit marks the
   // moment the slowest CTA finished the phase)
@@ -908,7 +911,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     if (!grid_sync(a.bar)) return;
     coarse_restrict<V, NP>(a, nullptr, true);
     if (!grid_sync(a.bar)) return;
-    coarse_solve<V, NP>(a, nullptr, true, reinterpret_cast<float*>(stage_raw), kStageBytes / 4);
+    coarse_solve<V, NP>(a, nullptr, true, reinterpret_cast<float*>(stage_raw), kStageBytes / 4, c_bytes);
   }
   if constexpr (PC == kPrecFactored) {  // r'z = ||G r||^2; P = G'(G r) below
     if (!grid_sync(a.bar)) return;
@@ -1198,7 +1201,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       coarse_restrict<V, NP>(a, st_cur, false);
       if (!grid_sync(a.bar)) return;
       mark(3);
-      coarse_solve<V, NP>(a, st_cur, false, reinterpret_cast<float*>(stage_raw), kStageBytes / 4);
+      coarse_solve<V, NP>(a, st_cur, false, reinterpret_cast<float*>(stage_raw), kStageBytes / 4, c_bytes);
       if (!grid_sync(a.bar)) return;
       mark(4);
     }
@@ -1327,6 +1330,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     atomicAdd(&a.work[0], w_rows);
     atomicAdd(&a.work[1], w_nnz);
   }
+  if (threadIdx.x == 0 && c_bytes != 0) atomicAdd(a.cwork, c_bytes);
 }
 
 // ---- sliced-ELL construction ---------------------------------------------
@@ -1515,9 +1519,9 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.bb = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
   a.state = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
   // control words: [2] iters, [5] err, [6..9] work (u64 x2), [10..11] ru_flag,
-  // [12] updates, [14..27] phase times (u64 x kPcgPhases); the barrier word
-  // sits alone on the next 128-byte line
-  static_assert(14 + 2 * kPcgPhases <= 32, "phase timers overlap the barrier line");
+  // [12] updates, [14..27] phase times (u64 x kPcgPhases), [28..29] coarse
+  // bytes (u64); the barrier word sits alone on the next 128-byte line
+  static_assert(14 + 2 * kPcgPhases <= 28, "phase timers overlap the coarse byte counter");
   unsigned* ctl = (unsigned*)w;
   w += a256(256);
   a.iters = (int*)(ctl + 2);
@@ -1526,6 +1530,7 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.work = (unsigned long long*)(ctl + 6);
   a.ru_flag = ctl + 10;
   a.n_updates = ctl + 12;
+  a.cwork = (unsigned long long*)(ctl + 28);
   a.part64 = (double*)w; w += a256(sizeof(double) * (size_t)ct.npiece * p);
   a.slot64 = (double*)w; w += a256(sizeof(double) * (size_t)ct.nslot * p);
   a.rref = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);
@@ -1605,7 +1610,10 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
     unsigned long long rows, nnz;
     memcpy(&rows, &hctl[6], 8);
     memcpy(&nnz, &hctl[8], 8);
-    lapy_profile_add_pcg(ms, (long long)hctl[2], (long long)rows, (long long)nnz, p, (int)sizeof(V));
+    unsigned long long cbytes;
+    memcpy(&cbytes, &hctl[28], 8);
+    lapy_profile_add_pcg(ms, (long long)hctl[2], (long long)rows, (long long)nnz, p, (int)sizeof(V), pc.kind,
+                         (double)cbytes);
     double phase_ms[kPcgPhases];
     for (int k = 0; k < kPcgPhases; ++k) {
       unsigned long long ns;

@@ -102,6 +102,7 @@ struct PcgPrecondDesc {
   const int32_t* agg = nullptr;       // n: aggregate of each row (-1: none)
   const int32_t* agg_ptr = nullptr;   // nagg + 1: member rows of each aggregate
   const int32_t* agg_row = nullptr;   //   (CSR, rows ascending)
+  int agg_contig = 0;                 // aggregate g is the row range [agg_ptr[g], agg_ptr[g+1])
   const int32_t* agg_sid = nullptr;   // nagg: segment of each aggregate
   const int32_t* seg_agg = nullptr;   // nseg + 1: aggregate range of each segment
   // (W'KW)^-1 of segment s = kscale[s] v v' + R, v = kvec[seg_agg[s] ..] the
