@@ -451,6 +451,103 @@ __device__ __forceinline__ void sell_unit_spmm(const SellMatrix<V>& M, const V* 
   }
 }
 
+// Asynchronous 16-byte global -> shared copies (completion tracked per
+// thread in commit groups).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Y = Mat * Xin over the units [u0, u1) of one piece from the FP32 SELL copy,
+// software-pipelined: while the warp gathers for unit u, the values and
+// column indices of unit u + 1 are already being copied into the other of
+// the warp's two shared-memory slots (cp.async), so a unit costs about one
+// memory round trip (its gathers).  Slices wider than kSellShort are read
+// directly.  `buf`: the warp's 2 * kSellShort * 32 values then as many column
+// indices.  With DOT, dacc[q] += Wdot(row, q) * Y(row, q).
+template <int NP, bool DOT>
+__device__ __forceinline__ void sell_piece_spmm(const SellMatrix<float>& M, const float* __restrict__ Xin,
+                                                float* __restrict__ Y, const float* __restrict__ Wdot,
+                                                const int32_t* __restrict__ unit_row, int u0, int u1,
+                                                float* __restrict__ buf, float (&dacc)[NP]) {
+  constexpr int kSlot = kSellShort * 32;
+  const int lane = threadIdx.x & 31;
+  float* sval = buf;
+  int32_t* scol = reinterpret_cast<int32_t*>(buf + 2 * kSlot);
+  // issue the copies of unit u's slice into slot `slot` (nothing for wide slices)
+  auto issue = [&](int32_t base, int w, int slot) {
+    if (w <= kSellShort) {
+      const int n16 = w * 8;  // 16-byte pieces per array (32 entries = 8 pieces per slice column)
+      for (int c = lane; c < n16; c += 32) {
+        cp_async16(sval + slot * kSlot + 4 * c, M.val + base + 4 * c);
+        cp_async16(scol + slot * kSlot + 4 * c, M.col + base + 4 * c);
+      }
+    }
+    cp_async_commit();
+  };
+  int32_t b0 = M.slice_ptr[u0], b1 = M.slice_ptr[u0 + 1];
+  int32_t b2 = (u0 + 1 < u1) ? M.slice_ptr[u0 + 2] : b1;
+  issue(b0, (b1 - b0) >> 5, 0);
+  for (int u = u0; u < u1; ++u) {
+    const int slot = (u - u0) & 1;
+    const int w = (b1 - b0) >> 5;
+    // next unit's slice into the other slot (every lane has finished reading
+    // it: the __syncwarp at the end of the previous iteration)
+    if (u + 1 < u1) issue(b1, (b2 - b1) >> 5, slot ^ 1);
+    else cp_async_commit();
+    const int32_t b3 = (u + 2 < u1) ? M.slice_ptr[u + 3] : b2;
+    float acc[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) acc[q] = 0.f;
+    if (w <= kSellShort) {
+      cp_async_wait_prev();  // this unit's group (all but the newest) is complete
+      __syncwarp();          // ... for every lane's copies
+      const float* sv = sval + slot * kSlot + lane;
+      const int32_t* sc = scol + slot * kSlot + lane;
+#pragma unroll
+      for (int k = 0; k < kSellShort; ++k) {
+        if (k < w) {
+          float xr[NP];
+          load_row<float, NP>(Xin, sc[32 * k], xr);
+          const float av = sv[32 * k];
+#pragma unroll
+          for (int q = 0; q < NP; ++q) acc[q] += av * xr[q];
+        }
+      }
+    } else {
+      const int32_t* __restrict__ cp = M.col + b0 + lane;
+      const float* __restrict__ vp = M.val + b0 + lane;
+#pragma unroll 4
+      for (int k = 0; k < w; ++k) {
+        const float a = __ldg(vp + 32 * k);
+        const int32_t c = __ldg(cp + 32 * k);
+        float xr[NP];
+        load_row<float, NP>(Xin, c, xr);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) acc[q] += a * xr[q];
+      }
+    }
+    const int row = unit_row[u] + lane;
+    if (row < unit_row[u + 1]) {
+      store_row<float, NP>(Y, row, acc);
+      if (DOT) {
+        float wv[NP];
+        load_row<float, NP>(Wdot, row, wv);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) dacc[q] += wv[q] * acc[q];
+      }
+    }
+    __syncwarp();  // the slot just read may be refilled next iteration
+    b0 = b1;
+    b1 = b2;
+    b2 = b3;
+  }
+  cp_async_wait_prev();
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 // Reduction slots.  After the warps of a CTA have stored the partial sums of
 // their pieces (and after a __syncthreads), the CTA folds them into one slot
 // per (segment, virtual CTA), one warp per segment, in piece order; consumers
@@ -831,7 +928,10 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
   using S = ScalarOf<V>;
   // one buffer: the SpMM's staged slices (values, then column indices) or,
   // in the coarse phase, a segment's restricted residual
-  constexpr int kStageBytes = kWarps * kStageWarp * (int)(sizeof(V) + sizeof(int32_t));
+  constexpr int kStageBytes =
+      kWarps * (kStageWarp * (int)(sizeof(V) + sizeof(int32_t)) > 2 * kSellShort * 32 * 8
+                    ? kStageWarp * (int)(sizeof(V) + sizeof(int32_t))
+                    : 2 * kSellShort * 32 * 8);
   __shared__ __align__(16) unsigned char stage_raw[kStageBytes];
   V* sval_all = reinterpret_cast<V*>(stage_raw);
   int32_t* sidx_all = reinterpret_cast<int32_t*>(stage_raw + kWarps * kStageWarp * sizeof(V));
@@ -839,6 +939,8 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
   const int gw = blockIdx.x * kWarps + warp, nw = gridDim.x * kWarps;
   V* wval = sval_all + warp * kStageWarp;
   int32_t* widx = sidx_all + warp * kStageWarp;
+  // the warp's two SELL slots (FP32 iterations)
+  float* wslots = reinterpret_cast<float*>(stage_raw) + warp * (2 * kSellShort * 32 * 2);
   S* part_pq = a.part;
   S* part_rz = a.part + (int64_t)a.npiece * NP;
   S* part_rr = a.part + 2 * (int64_t)a.npiece * NP;
@@ -1123,8 +1225,12 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       for (int q = 0; q < NP; ++q) acc[q] = S(0);
       if (any) {
         if (a.use_sell) {
-          for (int u = u0; u < u1; ++u)
-            sell_unit_spmm<V, NP, true>(a.sell, a.P, a.Q, a.P, u, a.unit_row[u], a.unit_row[u + 1], acc);
+          if constexpr (sizeof(V) == 4) {
+            sell_piece_spmm<NP, true>(a.sell, a.P, a.Q, a.P, a.unit_row, u0, u1, wslots, acc);
+          } else {
+            for (int u = u0; u < u1; ++u)
+              sell_unit_spmm<V, NP, true>(a.sell, a.P, a.Q, a.P, u, a.unit_row[u], a.unit_row[u + 1], acc);
+          }
         } else {
           for (int u = u0; u < u1; ++u)
             unit_spmm<V, NP, true>(a.indptr, a.indices, a.vals, a.P, a.Q, a.P, a.unit_row[u], a.unit_row[u + 1],
