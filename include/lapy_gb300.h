@@ -242,6 +242,37 @@ int lapy_pcg_solve_static(int64_t n, const int32_t* indptr, const int32_t* indic
                           int mixed, double inner_rtol, int32_t* status_out,
                           double* relres_out, int64_t* iters_out, void* stream);
 
+/* ---- incomplete Cholesky IC(0) -------------------------------------------
+ * No counterpart in the reference, which factors exactly (splu of A - sigma
+ * M at lapy/solver.py:707-712, of M + t A at lapy/heat.py:226): IC(0) is the
+ * incomplete factorization the GPU path offers as a preconditioner for the
+ * same SPD systems, beside Jacobi and the learned factor.
+ *
+ * lapy_ic0_factor: K (n x n CSR, sorted columns, full diagonal, f64) ~ L L'
+ * with L on K's own pattern.  l_vals (nnz) receives L on the lower part
+ * (columns <= row) and the mirror L[j][i] on each upper entry (i, j).  Rows
+ * are factored level by level (level of row i: 1 + the largest level of its
+ * lower neighbours); arithmetic in ascending column order without fused
+ * multiply-add.  A pivot that is not positive is replaced by K[i][i] and
+ * counted in *n_fixed (host).  n_levels (host, 2 ints): forward and backward
+ * level counts.  `work` (lapy_ic0_workspace_bytes(n, nnz, ncol)) keeps the
+ * level plan for later lapy_ic0_apply calls on the same matrix.
+ * lapy_ic0_apply: z = (L L')^-1 r for ncol row-major columns.
+ * lapy_ic0_pcg_solve: lapy_pcg_solve with the IC(0) preconditioner (factored
+ * inside; FP32 iterations in FP64 refinement); *n_fixed as above. */
+size_t lapy_ic0_workspace_bytes(int64_t n, int64_t nnz, int ncol);
+int lapy_ic0_factor(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
+                    int64_t nnz, double* l_vals, int32_t* n_fixed, int32_t* n_levels, void* work,
+                    size_t ws_bytes, void* stream);
+int lapy_ic0_apply(int64_t n, const int32_t* indptr, const int32_t* indices, const double* l_vals,
+                   int64_t nnz, int ncol, const double* r, double* z, void* work, size_t ws_bytes,
+                   void* stream);
+size_t lapy_ic0_pcg_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, int ncol);
+int lapy_ic0_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
+                       int64_t nnz, int nseg, const int32_t* seg_row, int ncol, const double* b, double* x,
+                       double rtol, int maxiter, double inner_rtol, int32_t* status_out, double* relres_out,
+                       int64_t* iters_out, int32_t* n_fixed, void* ws, size_t ws_bytes, void* stream);
+
 /* ---- generalized eigenproblem -------------------------------------------
  * Replaces Solver.eigs (lapy/solver.py:667-716): the k eigenpairs of
  * A x = lambda M x nearest sigma, by block shift-invert Lanczos (block width

@@ -287,3 +287,55 @@ def pcg_solve(indptr, indices, k_vals, n, nnz, b: torch.Tensor, rtol: float, max
     if bad.size:
         _lib.check(int(bad[0]), "pcg_solve")
     return (X[:, 0] if squeeze else X), relres, int(iters.value)
+
+
+def ic0_pcg_solve(indptr, indices, k_vals, n, nnz, b: torch.Tensor, rtol: float, maxiter: int = 20000,
+                  inner_rtol: float = 1e-4, seg_row=None):
+    """Solve K X = B with IC(0)-preconditioned PCG (FP32 iterations inside FP64
+    refinement); returns (X, relres, iters, replaced pivots)."""
+    L = _lib.lib()
+    squeeze = b.dim() == 1
+    B = b.reshape(n, -1).contiguous()
+    ncol = B.shape[1]
+    if seg_row is None:
+        seg_row = np.array([0, n], dtype=np.int32)
+    seg_row = np.ascontiguousarray(seg_row, dtype=np.int32)
+    nseg = len(seg_row) - 1
+    X = torch.empty_like(B)
+    ws = workspace(L.lapy_ic0_pcg_workspace_bytes(n, nnz, nseg, seg_row.ctypes.data, ncol))
+    status = np.zeros(nseg * ncol, dtype=np.int32)
+    relres = np.zeros(nseg * ncol, dtype=np.float64)
+    iters = C.c_int64(0)
+    fixed = C.c_int32(0)
+    _lib.check(L.lapy_ic0_pcg_solve(n, dptr(indptr), dptr(indices), dptr(k_vals), nnz, nseg, seg_row.ctypes.data,
+                                    ncol, dptr(B), dptr(X), rtol, maxiter, inner_rtol, status.ctypes.data,
+                                    relres.ctypes.data, C.byref(iters), C.byref(fixed), dptr(ws), ws.numel(),
+                                    stream()), "ic0_pcg_solve")
+    bad = status[status != 0]
+    if bad.size:
+        _lib.check(int(bad[0]), "ic0_pcg_solve")
+    return (X[:, 0] if squeeze else X), relres, int(iters.value), int(fixed.value)
+
+
+def ic0_factor(indptr, indices, k_vals, n, nnz):
+    """IC(0) factor of K on its own pattern (lower part L, upper part mirrored),
+    with the workspace that holds its level plan; returns (l_vals, work,
+    replaced pivots, (forward levels, backward levels))."""
+    L = _lib.lib()
+    lv = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    ws = workspace(L.lapy_ic0_workspace_bytes(n, nnz, 16))
+    fixed = C.c_int32(0)
+    levels = (C.c_int32 * 2)()
+    _lib.check(L.lapy_ic0_factor(n, dptr(indptr), dptr(indices), dptr(k_vals.contiguous()), nnz, dptr(lv),
+                                 C.byref(fixed), levels, dptr(ws), ws.numel(), stream()), "ic0_factor")
+    return lv, ws, int(fixed.value), (int(levels[0]), int(levels[1]))
+
+
+def ic0_apply(indptr, indices, l_vals, n, nnz, r: torch.Tensor, work: torch.Tensor) -> torch.Tensor:
+    """z = (L L')^-1 r with a factor from ic0_factor (r: n or n x ncol, ncol <= 16)."""
+    L = _lib.lib()
+    R = r.reshape(n, -1).contiguous()
+    Z = torch.empty_like(R)
+    _lib.check(L.lapy_ic0_apply(n, dptr(indptr), dptr(indices), dptr(l_vals), nnz, R.shape[1], dptr(R), dptr(Z),
+                                dptr(work), work.numel(), stream()), "ic0_apply")
+    return Z[:, 0] if r.dim() == 1 else Z

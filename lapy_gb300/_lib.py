@@ -101,6 +101,12 @@ _SIGNATURES = {
     "lapy_spai_pcg_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int]),
     "lapy_spai_pcg_solve": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _dbl, _int, _dbl, _vp, _vp,
                                    _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(_i64), _vp, _sz, _vp]),
+    "lapy_ic0_workspace_bytes": (_sz, [_i64, _i64, _int]),
+    "lapy_ic0_factor": (_int, [_i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "lapy_ic0_apply": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _vp, _vp, _sz, _vp]),
+    "lapy_ic0_pcg_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int]),
+    "lapy_ic0_pcg_solve": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _dbl, _int, _dbl, _vp, _vp,
+                                  C.POINTER(_i64), _vp, _vp, _sz, _vp]),
     "lapy_eigs_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int, _int, _int, _int]),
     "lapy_eigs_shift_invert": (_int, [_i64, _vp, _vp, _vp, _vp, _int, _i64, _int, _vp, _dbl, _int, _int,
                                       _int, _dbl, _dbl, _int, _int, C.c_uint64, _vp, _vp, _vp, _vp,

@@ -35,6 +35,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 EXTRA = {
     "assemble.cu": ["--fmad=false"],
     "geodesic.cu": ["--fmad=false"],
+    "ic0.cu": ["--fmad=false"],
 }
 
 

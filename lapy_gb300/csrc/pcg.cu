@@ -912,6 +912,71 @@ __device__ __forceinline__ void factor_first_half(const PcgArgs<V>& a, int u0, i
   }
 }
 
+// IC(0) preconditioner: T = L^-1 R level by level (one thread per row, a
+// grid barrier after each level), then Z = L^-T T over the backward levels.
+// Every row is solved (rows of converged segments too: their R is frozen).
+template <typename V, int NP>
+__device__ __forceinline__ bool ic0_apply_grid(const PcgArgs<V>& a) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  for (int l = 0; l < a.pc.ic_nlev_f; ++l) {
+    for (int32_t t = a.pc.ic_lev_f_ptr[l] + tid; t < a.pc.ic_lev_f_ptr[l + 1]; t += nth) {
+      const int32_t i = a.pc.ic_lev_f_row[t];
+      const int32_t kd = a.pc.ic_diag[i];
+      V acc[NP];
+      load_row<V, NP>(a.R, i, acc);
+      for (int32_t k = a.indptr[i]; k < kd; ++k) {
+        const V lv = a.pc.ic_val[k];
+        V y[NP];
+        load_row<V, NP>(a.T, a.indices[k], y);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) acc[q] -= lv * y[q];
+      }
+      const V d = a.pc.dinv[i];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] *= d;
+      store_row<V, NP>(a.T, i, acc);
+    }
+    if (!grid_sync(a.bar)) return false;
+  }
+  for (int l = 0; l < a.pc.ic_nlev_b; ++l) {
+    for (int32_t t = a.pc.ic_lev_b_ptr[l] + tid; t < a.pc.ic_lev_b_ptr[l + 1]; t += nth) {
+      const int32_t i = a.pc.ic_lev_b_row[t];
+      const int32_t kd = a.pc.ic_diag[i];
+      V acc[NP];
+      load_row<V, NP>(a.T, i, acc);
+      for (int32_t k = kd + 1; k < a.indptr[i + 1]; ++k) {
+        const V lv = a.pc.ic_val[k];
+        V z[NP];
+        load_row<V, NP>(a.Z, a.indices[k], z);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) acc[q] -= lv * z[q];
+      }
+      const V d = a.pc.dinv[i];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] *= d;
+      store_row<V, NP>(a.Z, i, acc);
+    }
+    if (!grid_sync(a.bar)) return false;
+  }
+  return true;
+}
+
+// Partial r'z of a piece's rows (z = Z, the preconditioned residual).
+template <typename V, int NP>
+__device__ __forceinline__ void piece_rz(const PcgArgs<V>& a, int u0, int u1, ScalarOf<V> (&acc)[NP]) {
+  const int lane = threadIdx.x & 31;
+  for (int u = u0; u < u1; ++u) {
+    const int row = a.unit_row[u] + lane;
+    if (row < a.unit_row[u + 1]) {
+      V r[NP], z[NP];
+      load_row<V, NP>(a.R, row, r);
+      load_row<V, NP>(a.Z, row, z);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] += r[q] * z[q];
+    }
+  }
+}
+
 // Loop over this warp's pieces: s = segment, [u0, u1) = units of the piece.
 #define FOR_MY_PIECES(a, ...)                                                               \
   for (int vw = gw; vw < (a).nvw; vw += nw) {                                                \
@@ -1015,6 +1080,21 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     if (!grid_sync(a.bar)) return;
     coarse_solve<V, NP>(a, nullptr, true, reinterpret_cast<float*>(stage_raw), kStageBytes / 4, c_bytes);
   }
+  if constexpr (PC == kPrecIC0) {  // Z = (L L')^-1 R, r'z; P = Z below
+    if (!grid_sync(a.bar)) return;
+    if (!ic0_apply_grid<V, NP>(a)) return;
+    FOR_MY_PIECES(a, {
+      S acc[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) acc[q] = S(0);
+      piece_rz<V, NP>(a, u0, u1, acc);
+      warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
+    })
+    if (a.fold) {
+      __syncthreads();
+      fold_pieces<V, NP>(a, part_rz, slot_rz);
+    }
+  }
   if constexpr (PC == kPrecFactored) {  // r'z = ||G r||^2; P = G'(G r) below
     if (!grid_sync(a.bar)) return;
     FOR_MY_PIECES(a, {
@@ -1039,6 +1119,16 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
         V z[NP];
         row_apply<V, NP>(a.pc.gt_sell, a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, u, row, valid, z);
         if (valid) store_row<V, NP>(a.P, row, z);
+      }
+    }
+    if constexpr (PC == kPrecIC0) {
+      for (int u = u0; u < u1; ++u) {
+        const int row = a.unit_row[u] + lane;
+        if (row < a.unit_row[u + 1]) {
+          V z[NP];
+          load_row<V, NP>(a.Z, row, z);
+          store_row<V, NP>(a.P, row, z);
+        }
       }
     }
     if constexpr (PC == kPrecTwoLevel) {
@@ -1312,6 +1402,24 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       mark(4);
     }
 
+    if constexpr (PC == kPrecIC0) {
+      // ---- phase B2: Z = (L L')^-1 R by level-scheduled solves, then r'z
+      if (!ic0_apply_grid<V, NP>(a)) return;
+      FOR_MY_PIECES(a, {
+        S acc[NP];
+#pragma unroll
+        for (int q = 0; q < NP; ++q) acc[q] = S(0);
+        piece_rz<V, NP>(a, u0, u1, acc);
+        warp_store_partials<NP>(acc, part_rz + (int64_t)p * NP);
+      })
+      if (a.fold) {
+        __syncthreads();
+        fold_pieces<V, NP>(a, part_rz, slot_rz);
+      }
+      if (!grid_sync(a.bar)) return;
+      mark(3);
+    }
+
     if constexpr (PC == kPrecFactored) {
       // ---- phase B2: T = G R and r'z = ||T||^2 (G'T is applied in phase C)
       FOR_MY_PIECES(a, {
@@ -1388,6 +1496,8 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
               V r[NP];
               load_row<V, NP>(a.R, row, r);
               apply_diag_coarse<V, NP, PC>(a, row, r, z);
+            } else if constexpr (PC == kPrecIC0) {
+              load_row<V, NP>(a.Z, row, z);
             } else {
               row_apply<V, NP>(a.pc.gt_sell, a.pc.gt_ptr, a.pc.gt_idx, a.pc.gt_val, a.T, u, row, true, z);
             }
@@ -1521,7 +1631,7 @@ template int build_sell<double>(int64_t, const int32_t*, const int32_t*, const d
 
 size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond, int64_t nagg) {
   const size_t vec = a256((size_t)n * p * elem_size);
-  size_t b = vec * (precond == kPrecFactored ? 4 : 3);  // R P Q (+ T)
+  size_t b = vec * (precond == kPrecFactored ? 4 : precond == kPrecIC0 ? 5 : 3);  // R P Q (+ T, + Z)
   b += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
   b += a256(sizeof(double) * 3 * (size_t)ct.nslot * p);
   b += a256(sizeof(double) * (size_t)ct.nslot * p);
@@ -1615,8 +1725,11 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.Q = (V*)w; w += vec;
   a.Z = nullptr;
   a.T = nullptr;
-  if (pc.kind == kPrecFactored) {
+  if (pc.kind == kPrecFactored || pc.kind == kPrecIC0) {
     a.T = (V*)w; w += vec;
+  }
+  if (pc.kind == kPrecIC0) {
+    a.Z = (V*)w; w += vec;
   }
   using S = ScalarOf<V>;
   a.part = (S*)w; w += a256(sizeof(double) * 3 * (size_t)ct.npiece * p);
@@ -1693,6 +1806,13 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
     }
   } else if (pc.kind == kPrecFactored) {
     st = launch_pcg_np<V, kPrecFactored>(a, p, stream);
+  } else if (pc.kind == kPrecIC0) {
+    if constexpr (sizeof(V) == 4) {
+      st = launch_pcg_np<V, kPrecIC0>(a, p, stream);
+    } else {
+      lapy_set_last_message("pcg: the IC(0) preconditioner runs FP32 iterations");
+      return LAPY_ERR_INVALID;
+    }
   } else if (pc.kind == kPrecTwoLevel) {
     if constexpr (sizeof(V) == 4) {
       st = launch_pcg_np<V, kPrecTwoLevel>(a, p, stream);

@@ -50,7 +50,7 @@ size_t chunk_table_bytes(const ChunkTable& ct);
 // Place the table into `mem` and upload it (synchronous on `stream`).
 int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream);
 
-enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1, kPrecTwoLevel = 2 };
+enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1, kPrecTwoLevel = 2, kPrecIC0 = 3 };
 
 // Coarse rows per coarse-solve task: 8 warps x 4 rows; a warp computes
 // kCoarseRowsPerPass of them at a time (block widths up to 4).
@@ -103,6 +103,16 @@ struct PcgPrecondDesc {
   const int32_t* agg_ptr = nullptr;   // nagg + 1: member rows of each aggregate
   const int32_t* agg_row = nullptr;   //   (CSR, rows ascending)
   int agg_contig = 0;                 // aggregate g is the row range [agg_ptr[g], agg_ptr[g+1])
+  // IC(0): z = L^-T L^-1 r with L on the system's own CSR pattern (lower
+  // part L, upper part the mirror L[j][i]); dinv holds 1 / L[i][i]; rows in
+  // forward / backward level order (level l: [ptr[l], ptr[l+1]))
+  const V* ic_val = nullptr;
+  const int32_t* ic_diag = nullptr;
+  int ic_nlev_f = 0, ic_nlev_b = 0;
+  const int32_t* ic_lev_f_ptr = nullptr;
+  const int32_t* ic_lev_f_row = nullptr;
+  const int32_t* ic_lev_b_ptr = nullptr;
+  const int32_t* ic_lev_b_row = nullptr;
   const int32_t* agg_sid = nullptr;   // nagg: segment of each aggregate
   const int32_t* seg_agg = nullptr;   // nseg + 1: aggregate range of each segment
   // (W'KW)^-1 of segment s = kscale[s] v v' + R, v = kvec[seg_agg[s] ..] the

@@ -3,6 +3,7 @@
 #include <mutex>
 #include <vector>
 #include "blas.cuh"
+#include "ic0.cuh"
 #include "solve.cuh"
 #include "spmv.cuh"
 
@@ -129,7 +130,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
       }
       int it = 0;
       PcgPrecondDesc<float> pc = K.pc32;
-      if (pc.kind != kPrecFactored) pc.dinv = K.dinv32;
+      if (pc.kind == kPrecJacobi || pc.kind == kPrecTwoLevel) pc.dinv = K.dinv32;
       LAPY_TRY(pcg_solve<float>(n, K.indptr, K.indices, K.k32, K.sell32.val ? &K.sell32 : nullptr, pc, p, ct, R32,
                                 D32, round_rtol, maxiter, st, pws, pws_bytes, stream, &it));
       local.rounds++;
@@ -304,14 +305,25 @@ static size_t factor_sell_bytes(int64_t n, int64_t nnz, int nseg, const int32_t*
   return 2 * sell_bytes_bound((nnz + n) / 2, ct, sizeof(float), kFactorPad) + 512;
 }
 
+// Device memory of the IC(0) preconditioner of an n-row system: level plan,
+// FP64 factor, its FP32 copy, 1 / L[i][i] and a pivot counter.
+static size_t ic0_pre_bytes(int64_t n, int64_t nnz) {
+  return ic0_plan_bytes(n) + a256(8 * (size_t)nnz) + a256(4 * (size_t)nnz) + a256(4 * (size_t)n) + a256(64) + 256;
+}
+
 // Shared body of the PCG entry points; `factored` (may be null) selects the
-// factored preconditioner z = G' (G r) with FP32 factors on CSR patterns.
+// factored preconditioner z = G' (G r) with FP32 factors on CSR patterns;
+// `ic0` the IC(0) preconditioner, factored here (*ic0_fixed: pivots replaced).
 static int pcg_solve_impl(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
                           int64_t nnz, int nseg, const int32_t* seg_row, int ncol, const double* b, double* x,
                           double rtol, int maxiter, int mixed, double inner_rtol, int32_t* status_out,
                           double* relres_out, int64_t* iters_out, void* ws, size_t ws_bytes, cudaStream_t stream,
-                          const PcgPrecondDesc<float>* factored) {
-  const int precond = factored ? kPrecFactored : kPrecJacobi;
+                          const PcgPrecondDesc<float>* factored, bool ic0 = false, int32_t* ic0_fixed = nullptr) {
+  const int precond = factored ? kPrecFactored : ic0 ? kPrecIC0 : kPrecJacobi;
+  if (ic0 && !mixed) {
+    lapy_set_last_message("pcg_solve: the IC(0) preconditioner runs inside the mixed-precision solve");
+    return LAPY_ERR_INVALID;
+  }
   if (n <= 0 || !indptr || !indices || !k_vals || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0 ||
       !b || !x || !(rtol > 0) || maxiter <= 0 || !ws) {
     lapy_set_last_message("pcg_solve: invalid arguments");
@@ -324,7 +336,9 @@ static int pcg_solve_impl(int64_t n, const int32_t* indptr, const int32_t* indic
   const size_t main_bytes = solve_layout(n, nnz, nseg, ncol, mixed, precond, nullptr, nullptr, nullptr, nullptr,
                                          nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
                                          nullptr, nullptr, seg_row);
-  if (ws_bytes < main_bytes + (factored ? factor_sell_bytes(n, nnz, nseg, seg_row) : 0)) return LAPY_ERR_WORKSPACE;
+  if (ws_bytes < main_bytes + (factored ? factor_sell_bytes(n, nnz, nseg, seg_row) : 0) +
+                     (ic0 ? ic0_pre_bytes(n, nnz) : 0))
+    return LAPY_ERR_WORKSPACE;
   int32_t* diag_pos;
   double *dinv64, *Bp, *Xp;
   float *dinv32, *k32;
@@ -360,6 +374,36 @@ static int pcg_solve_impl(int64_t n, const int32_t* indptr, const int32_t* indic
     LAPY_TRY(build_sell<float>(n, factored->gt_ptr, factored->gt_idx, factored->gt_val, ct, gmem + gsb, gsb,
                                &K.pc32.gt_sell, &fits, stream));
     if (!fits) K.pc32.gt_sell = SellMatrix<float>();
+  }
+  if (ic0) {
+    char* w = base + a256(main_bytes);
+    const size_t pb = ic0_plan_bytes(n);
+    Ic0Plan plan;
+    LAPY_TRY(ic0_plan(n, indptr, indices, w, pb, &plan, stream));
+    char* w2 = (char*)(((uintptr_t)w + 255) & ~uintptr_t(255)) + pb;
+    double* L64 = (double*)w2; w2 += a256(8 * (size_t)nnz);
+    float* L32 = (float*)w2; w2 += a256(4 * (size_t)nnz);
+    float* dinv_ic = (float*)w2; w2 += a256(4 * (size_t)n);
+    unsigned* fixed_dev = (unsigned*)w2;
+    LAPY_CUDA_TRY(cudaMemsetAsync(L64, 0, 8 * (size_t)nnz, stream));
+    LAPY_TRY(ic0_factor(plan, indptr, indices, k_vals, L64, fixed_dev, stream));
+    LAPY_TRY(ic0_to_f32(plan, L64, nnz, L32, dinv_ic, stream));
+    unsigned fx = 0;
+    LAPY_CUDA_TRY(cudaMemcpyAsync(&fx, fixed_dev, sizeof(fx), cudaMemcpyDeviceToHost, stream));
+    LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (ic0_fixed) *ic0_fixed = (int32_t)fx;
+    PcgPrecondDesc<float> pc;
+    pc.kind = kPrecIC0;
+    pc.dinv = dinv_ic;
+    pc.ic_val = L32;
+    pc.ic_diag = plan.diag_pos;
+    pc.ic_nlev_f = plan.nlev_f;
+    pc.ic_nlev_b = plan.nlev_b;
+    pc.ic_lev_f_ptr = plan.lev_f_ptr;
+    pc.ic_lev_f_row = plan.lev_f_row;
+    pc.ic_lev_b_ptr = plan.lev_b_ptr;
+    pc.ic_lev_b_row = plan.lev_b_row;
+    K.pc32 = pc;
   }
   if (mixed) {
     bool fits = false;
@@ -427,6 +471,23 @@ extern "C" int lapy_spai_pcg_solve(int64_t n, const int32_t* indptr, const int32
   pc.gt_val = g_upper;
   return pcg_solve_impl(n, indptr, indices, k_vals, nnz, nseg, seg_row, ncol, b, x, rtol, maxiter, 1, inner_rtol,
                         status_out, relres_out, iters_out, ws, ws_bytes, (cudaStream_t)stream, &pc);
+}
+
+extern "C" size_t lapy_ic0_pcg_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row, int ncol) {
+  if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || ncol <= 0) return 0;
+  return a256(solve_layout(n, nnz, nseg, ncol, 1, kPrecIC0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                           nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, seg_row)) +
+         ic0_pre_bytes(n, nnz) + 256;
+}
+
+extern "C" int lapy_ic0_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
+                                  int64_t nnz, int nseg, const int32_t* seg_row, int ncol, const double* b,
+                                  double* x, double rtol, int maxiter, double inner_rtol, int32_t* status_out,
+                                  double* relres_out, int64_t* iters_out, int32_t* n_fixed, void* ws,
+                                  size_t ws_bytes, void* stream) {
+  return pcg_solve_impl(n, indptr, indices, k_vals, nnz, nseg, seg_row, ncol, b, x, rtol, maxiter, 1, inner_rtol,
+                        status_out, relres_out, iters_out, ws, ws_bytes, (cudaStream_t)stream, nullptr, true,
+                        n_fixed);
 }
 
 // ---------------------------------------------------------------------------

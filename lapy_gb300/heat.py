@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._device import axpby, dptr, pcg_solve, require_cuda, stream
+from ._device import axpby, dptr, ic0_pcg_solve, pcg_solve, require_cuda, stream
 
 logger = logging.getLogger(__name__)
 
@@ -81,10 +81,11 @@ def diffusion(geometry, vids, m: float = 1.0, aniso=None, use_cholmod: bool = Fa
               precond: str = "jacobi"):
     """Heat diffusion from the vertices in ``vids`` (same semantics as the reference).
 
-    ``precond``: ``"jacobi"`` or ``"learned"`` (the shipped per-edge MLP
-    sparse approximate inverse; isotropic systems only)."""
-    if precond not in ("jacobi", "learned"):
-        raise ValueError(f"precond must be 'jacobi' or 'learned', not {precond!r}")
+    ``precond``: ``"jacobi"``, ``"ic0"`` (incomplete Cholesky) or ``"learned"``
+    (the shipped per-edge MLP sparse approximate inverse; isotropic systems
+    only)."""
+    if precond not in ("jacobi", "ic0", "learned"):
+        raise ValueError(f"precond must be 'jacobi', 'ic0' or 'learned', not {precond!r}")
     if precond == "learned" and aniso is not None:
         raise ValueError("the learned preconditioner covers isotropic systems (aniso=None)")
     if use_cholmod:
@@ -125,6 +126,8 @@ def diffusion(geometry, vids, m: float = 1.0, aniso=None, use_cholmod: bool = Fa
 
         sysg = SpaiSystems(BatchInput([geometry]), "heat", t=[t])
         x, relres, iters = learned_solve(sysg, B, rtol)
+    elif precond == "ic0":
+        x, relres, iters, _ = ic0_pcg_solve(A.indptr, A.indices, hvals, n, hvals.numel(), B, rtol)
     else:
         x, relres, iters = pcg_solve(A.indptr, A.indices, hvals, n, hvals.numel(), B, rtol)
     logger.debug("heat solve: %d PCG iterations, max rel. residual %.2e", iters, float(np.max(relres)))
@@ -167,7 +170,7 @@ class HeatBatch:
 
     def solve(self, rtol: float = 1e-11, maxiter: int = 20000, precond: str = "jacobi"):
         """Assemble and solve every segment; returns (u (n,), info).
-        ``precond``: ``"jacobi"`` or ``"learned"`` (per-edge MLP SPAI)."""
+        ``precond``: ``"jacobi"``, ``"ic0"`` or ``"learned"`` (per-edge MLP SPAI)."""
         from .shapedna import BatchedFEM
 
         inp = self.input
@@ -191,8 +194,11 @@ class HeatBatch:
         elif precond == "jacobi":
             x, relres, iters = pcg_solve(fem.indptr, fem.indices, hvals, fem.n, fem.nnz, self.b0, rtol, maxiter,
                                          seg_row=inp.seg_row)
+        elif precond == "ic0":
+            x, relres, iters, _ = ic0_pcg_solve(fem.indptr, fem.indices, hvals, fem.n, fem.nnz, self.b0, rtol,
+                                                maxiter, seg_row=inp.seg_row)
         else:
-            raise ValueError(f"precond must be 'jacobi' or 'learned', not {precond!r}")
+            raise ValueError(f"precond must be 'jacobi', 'ic0' or 'learned', not {precond!r}")
         return x, {"relres": relres, "iters": iters, "t": t, "avg_edge_length": avg}
 
 

@@ -199,11 +199,16 @@ class SpaiSystems:
                    "spai_transpose_values")
         return g, gt, logq, dldw
 
-    def solve(self, B: torch.Tensor, g=None, gt=None, rtol: float = 1e-8, maxiter: int = 20000):
-        """PCG on every segment: the learned factor (g, gt) or Jacobi (None).
-        Returns (X, relres per (segment, column), PCG iterations)."""
-        from ._device import pcg_solve
+    def solve(self, B: torch.Tensor, g=None, gt=None, rtol: float = 1e-8, maxiter: int = 20000, ic0: bool = False):
+        """PCG on every segment: the learned factor (g, gt), IC(0) (ic0=True)
+        or Jacobi (neither).  Returns (X, relres per (segment, column), PCG
+        iterations)."""
+        from ._device import ic0_pcg_solve, pcg_solve
 
+        if ic0:
+            x, relres, iters, _ = ic0_pcg_solve(self.indptr, self.indices, self.k, self.n, self.nnz, B, rtol, maxiter,
+                                                seg_row=self.input.seg_row)
+            return x, relres, iters
         if g is None:
             return pcg_solve(self.indptr, self.indices, self.k, self.n, self.nnz, B, rtol, maxiter,
                              seg_row=self.input.seg_row)
