@@ -271,13 +271,28 @@ def run_gpu(args, rank, world):
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     meshes, lv = make_batch(args.meshes, seed=rank_seed(args.seed, rank))
+    # solver knobs: calibrated for this batch's shape class on this device
+    # (stratified sample, untimed) unless --block fixes the block width
+    from lapy_gb300 import autotune
+
+    tune_info = None
+    if args.block:
+        choice = dict(autotune.DEFAULT, block=args.block)
+    else:
+        t0 = time.perf_counter()
+        choice, report = autotune.calibrate(meshes, k=K_EIG, sample=args.tune_sample)
+        tune_info = {"sample_meshes": min(args.tune_sample, len(meshes)), "trials": len(report),
+                     "calibration_s": time.perf_counter() - t0,
+                     "trial_seconds": [[c, round(t, 4)] for c, t in report]}
+    block = int(choice["block"])
+    tuning = autotune.solver_tuning(choice)
     # inputs resident in HBM before the timed region
     batch_in = shapedna.BatchInput(meshes)
     torch.cuda.synchronize()
 
     def step():
         fem = shapedna.BatchedFEM.from_input(batch_in, lump=False)
-        evals, _, info = fem.eigs(k=K_EIG, block=args.block)
+        evals, _, info = fem.eigs(k=K_EIG, block=block, tuning=tuning)
         return evals, info
 
     for _ in range(args.warmup):
@@ -313,7 +328,7 @@ def run_gpu(args, rank, world):
     e2e_steps = 0 if args.no_e2e else args.e2e_steps
     te = time.perf_counter()
     for _ in range(e2e_steps):
-        res = shapedna.compute_shapedna_batch(meshes, k=K_EIG, block=args.block, return_vectors=False)
+        res = shapedna.compute_shapedna_batch(meshes, k=K_EIG, block=block, tuning=tuning, return_vectors=False)
     torch.cuda.synchronize()
     te = time.perf_counter() - te
     h2d = sum(m.v.nbytes + m.t.size * 4 for m in meshes)
@@ -328,12 +343,12 @@ def run_gpu(args, rank, world):
         "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 inner PCG / f64 Lanczos, Ritz and refinement", "data": "synthetic",
         "config": {"workload": workload_name(args.meshes, n_total),
-                   "block": args.block, "per_gpu_meshes": args.meshes,
+                   "block": block, "tuning": choice, "autotune": tune_info, "per_gpu_meshes": args.meshes,
                    "l2": "inputs larger than L2 (batch CSR + Krylov basis >> 129 MB)",
                    "parallelism": f"replicas x{world} (meshes sharded, no collective)"},
         "e2e": ({"value": world * args.meshes * e2e_steps / te, "unit": "spectra/s", "h2d_bytes_per_step": h2d,
                  "d2h_bytes_per_step": d2h, "calls": e2e_steps} if e2e_steps else None),
-        "roofline": {"bound": "hbm", "kernel": "pcg_kernel (persistent FP32 Jacobi-PCG)",
+        "roofline": {"bound": "hbm", "kernel": "pcg_kernel (persistent FP32 two-level PCG)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": None,
                      "peak_kind": f"{peak_kind} hbm_gbs",
@@ -707,7 +722,8 @@ def main():
     ap.add_argument("--workload", default="shapedna", choices=["shapedna", "sphere-l5", "kuhn-64", "sphere-l8-geodesics"],
                     help="shapedna: the batched headline (512 meshes); the others: single-mesh workloads")
     ap.add_argument("--meshes", type=int, default=512)
-    ap.add_argument("--block", type=int, default=4)
+    ap.add_argument("--block", type=int, default=0, help="Lanczos block width; 0: autotuned with the other knobs")
+    ap.add_argument("--tune-sample", type=int, default=32, help="meshes of the autotuner's calibration sample")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-per-level", type=int, default=4)
     ap.add_argument("--plain-per-level", type=int, default=1)

@@ -296,6 +296,29 @@ int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const int32_t* indi
                            int inner_maxiter, int precond, uint64_t seed, double* evals, double* evecs,
                            int32_t* status_out, int32_t* nbasis_out, int64_t* inner_iters_out,
                            void* ws, size_t ws_bytes, void* stream);
+/* lapy_eigs_shift_invert with the solver's tunable knobs (the reference has no
+ * counterpart: ARPACK and SuperLU have none of these).  Zero fields keep the
+ * defaults; tuning == NULL is lapy_eigs_shift_invert.  Results agree with
+ * the defaults' to the eigenvalue tolerance; only the time changes.
+ *   agg_target   rows per aggregate of the two-level coarse space (64..1024)
+ *   round_rtol   residual reduction of each FP32 refinement round (0..1)
+ *   fold_pieces  fold PCG partial sums per CTA above this many pieces
+ *   fold_aggs    ... above this many coarse unknowns per segment
+ *   ctas_per_sm  resident PCG CTAs per SM to launch (1..5) */
+typedef struct lapy_eigs_tuning {
+  int agg_target;
+  double round_rtol;
+  int fold_pieces;
+  int fold_aggs;
+  int ctas_per_sm;
+} lapy_eigs_tuning;
+int lapy_eigs_shift_invert_tuned(int64_t n, const int32_t* indptr, const int32_t* indices,
+                                 const double* a_vals, const double* m_vals, int m_is_diag, int64_t nnz,
+                                 int nseg, const int32_t* seg_row, double sigma, int k, int block,
+                                 int max_vectors, double tol, double inner_rtol, int inner_maxiter,
+                                 int precond, uint64_t seed, double* evals, double* evecs,
+                                 int32_t* status_out, int32_t* nbasis_out, int64_t* inner_iters_out,
+                                 void* ws, size_t ws_bytes, void* stream, const lapy_eigs_tuning* tuning);
 
 /* ---- learned sparse approximate inverse (per-edge MLP) -------------------
  * No counterpart in the reference (it factorises with splu).  For an SPD

@@ -39,6 +39,13 @@ class ConvergenceError(LapyGpuError):
     """An iterative solve hit its iteration cap (LAPY_ERR_NOCONV)."""
 
 
+class EigsTuning(C.Structure):
+    """``lapy_eigs_tuning`` (include/lapy_gb300.h): zero fields keep the defaults."""
+
+    _fields_ = [("agg_target", C.c_int), ("round_rtol", C.c_double), ("fold_pieces", C.c_int),
+                ("fold_aggs", C.c_int), ("ctas_per_sm", C.c_int)]
+
+
 _i32p = C.c_void_p
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -108,6 +115,9 @@ _SIGNATURES = {
     "lapy_ic0_pcg_solve": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _dbl, _int, _dbl, _vp, _vp,
                                   C.POINTER(_i64), _vp, _vp, _sz, _vp]),
     "lapy_eigs_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int, _int, _int, _int]),
+    "lapy_eigs_shift_invert_tuned": (_int, [_i64, _vp, _vp, _vp, _vp, _int, _i64, _int, _vp, _dbl, _int, _int,
+                                            _int, _dbl, _dbl, _int, _int, C.c_uint64, _vp, _vp, _vp, _vp,
+                                            C.POINTER(_i64), _vp, _sz, _vp, C.POINTER(EigsTuning)]),
     "lapy_eigs_shift_invert": (_int, [_i64, _vp, _vp, _vp, _vp, _int, _i64, _int, _vp, _dbl, _int, _int,
                                       _int, _dbl, _dbl, _int, _int, C.c_uint64, _vp, _vp, _vp, _vp,
                                       C.POINTER(_i64), _vp, _sz, _vp]),

@@ -23,8 +23,9 @@ static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Aggregate size for a segment of `rows` rows: kAggTarget, grown for large
 // segments so that the coarse dimension stays below about 0.8 kCoarseMaxDim.
-static int seg_target(int64_t rows) {
-  return (int)std::max<int64_t>(kAggTarget, (rows * 5 + 4 * kCoarseMaxDim - 1) / (4 * kCoarseMaxDim));
+static int seg_target(int64_t rows, int agg_target = kAggTarget) {
+  return (int)std::max<int64_t>(std::max(agg_target, kAggTarget),
+                                (rows * 5 + 4 * kCoarseMaxDim - 1) / (4 * kCoarseMaxDim));
 }
 // Largest accepted coarse dimension: aggregates average at least 5/8 of the target.
 static int64_t seg_cap(int64_t rows) {
@@ -68,10 +69,10 @@ size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg, int nvc) {
 // ---- host aggregation -------------------------------------------------------
 // Labels rows [r0, r1) with local aggregate ids 0..nc-1 (lab: global array).
 static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, const int32_t* indices,
-                             int32_t* lab) {
+                             int32_t* lab, int agg_target) {
   const int32_t len = r1 - r0;
   if (len <= 0) return 0;
-  const int target = seg_target(len);
+  const int target = seg_target(len, agg_target);
   for (int32_t v = r0; v < r1; ++v) lab[v] = -1;
   std::vector<int32_t> queue;
   queue.reserve(target);
@@ -333,7 +334,7 @@ static int host_threads(int nseg) {
 }
 
 int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, const int32_t* seg_row, int nseg,
-                         int32_t* perm, int32_t* lab_new) {
+                         int32_t* perm, int32_t* lab_new, int agg_target) {
   std::vector<int32_t> lab(n, -1);
   const int nthr = host_threads(nseg);
   std::vector<std::thread> pool;
@@ -342,7 +343,7 @@ int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, co
       std::vector<int32_t> order, first, cnt, fill, agg_order, agg_rank, queue;
       for (int s = t; s < nseg; s += nthr) {
         const int32_t r0 = seg_row[s], r1 = seg_row[s + 1];
-        const int nc = aggregate_segment(r0, r1, hptr, hidx, lab.data());
+        const int nc = aggregate_segment(r0, r1, hptr, hidx, lab.data(), agg_target);
         if (nc <= 0) {  // no coarse space: rows keep their order, no aggregate
           for (int32_t v = r0; v < r1; ++v) {
             perm[v] = v;
@@ -399,7 +400,7 @@ int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, co
 
 int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64,
                     const int32_t* seg_row, int nseg, int nvc, void* mem, size_t bytes,
-                    PcgPrecondDesc<float>* pc, cudaStream_t stream, const int32_t* lab_in) {
+                    PcgPrecondDesc<float>* pc, cudaStream_t stream, const int32_t* lab_in, int agg_target) {
   nvc = std::max(nvc, 1);
   if (bytes < two_level_bytes(n, seg_row, nseg, nvc)) return LAPY_ERR_WORKSPACE;
   std::vector<int32_t> lab(n, -1), nc(nseg, 0);
@@ -431,7 +432,7 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
     for (int t = 0; t < nthr; ++t)
       pool.emplace_back([&, t]() {
         for (int s = t; s < nseg; s += nthr)
-          nc[s] = aggregate_segment(seg_row[s], seg_row[s + 1], hptr.data(), hidx.data(), lab.data());
+          nc[s] = aggregate_segment(seg_row[s], seg_row[s + 1], hptr.data(), hidx.data(), lab.data(), agg_target);
       });
     for (auto& th : pool) th.join();
   }

@@ -30,7 +30,8 @@ size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg, int nvc);
 // (plan_aggregate_order), used instead of aggregating here.
 int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64,
                     const int32_t* seg_row, int nseg, int nvc, void* mem, size_t bytes,
-                    PcgPrecondDesc<float>* pc, cudaStream_t stream, const int32_t* lab_in = nullptr);
+                    PcgPrecondDesc<float>* pc, cudaStream_t stream, const int32_t* lab_in = nullptr,
+                    int agg_target = kAggTarget);
 
 // Row order of a batch (host, pattern on the host) that makes every
 // aggregate a contiguous row range: each segment is aggregated as
@@ -40,7 +41,9 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
 // aggregate id in the new order (-1 for segments without a coarse space,
 // whose rows keep their order).  Neighbouring rows thereby sit in the same
 // or nearby aggregates, so the gathers of a sparse product stay close.
+// agg_target: rows per aggregate (at least kAggTarget, which the workspace
+// bounds assume).
 int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, const int32_t* seg_row, int nseg,
-                         int32_t* perm, int32_t* lab_new);
+                         int32_t* perm, int32_t* lab_new, int agg_target = kAggTarget);
 
 }  // namespace lapy

@@ -702,6 +702,8 @@ struct EigPlan {
   int64_t n, nnz;
   int nseg, p, k, keff, mb, lda;
   int precond = kPrecJacobi;  // inner PCG: Jacobi or two-level
+  int agg_target = kAggTarget;  // rows per aggregate (two-level)
+  PcgTuning pcg;                // launch knobs of the inner PCG
   int64_t nagg_max = 0;
   ChunkTable ct;   // PCG chunks
   ChunkTable gt;   // GEMM chunks (larger)
@@ -989,7 +991,7 @@ static int reorder_system(const EigPlan& P, const EigPtrs& e, const int32_t** in
   std::vector<int32_t> perm(n), nptr(n + 1, 0);
   lab_out->assign(n, -1);
   LAPY_TRY(plan_aggregate_order(n, hptr.data(), hidx.data(), P.ct.h_seg_row.data(), P.nseg, perm.data(),
-                                lab_out->data()));
+                                lab_out->data(), P.agg_target));
   for (int64_t i = 0; i < n; ++i) nptr[i + 1] = nptr[i] + (hptr[perm[i] + 1] - hptr[perm[i]]);
   LAPY_CUDA_TRY(cudaMemcpyAsync(e.perm, perm.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, st));
   LAPY_CUDA_TRY(cudaMemcpyAsync(e.pindptr, nptr.data(), 4 * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
@@ -1042,6 +1044,7 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   LAPY_TRY(cast_f64_f32(P.nnz, e.k64, e.k32, st));
   LAPY_TRY(jacobi_inverse(n, e.diag_pos, e.k64, e.dinv64, e.dinv32, st));
   SysMatrix K;
+  K.tuning = P.pcg;
   K.n = n; K.nnz = P.nnz; K.indptr = indptr; K.indices = indices;
   K.k64 = e.k64; K.k32 = e.k32; K.dinv64 = e.dinv64; K.dinv32 = e.dinv32;
   {
@@ -1061,7 +1064,7 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   }
   if (P.precond == kPrecTwoLevel)
     LAPY_TRY(build_two_level(n, indptr, indices, e.k64, P.ct.h_seg_row.data(), ns, P.ct.nvc, e.tl_mem,
-                             e.tl_bytes, &K.pc32, st, reorder ? lab.data() : nullptr));
+                             e.tl_bytes, &K.pc32, st, reorder ? lab.data() : nullptr, P.agg_target));
 
   LAPY_CUDA_TRY(cudaMemsetAsync(e.rcnt, 0, 16, st));
   std::vector<int32_t> hact(ns, 1), hnsize(ns, 0);
@@ -1278,6 +1281,33 @@ extern "C" int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const in
                                       int precond, uint64_t seed, double* evals, double* evecs, int32_t* status_out,
                                       int32_t* nbasis_out, int64_t* inner_iters_out, void* ws, size_t ws_bytes,
                                       void* stream) {
+  return lapy_eigs_shift_invert_tuned(n, indptr, indices, a_vals, m_vals, m_is_diag, nnz, nseg, seg_row, sigma, k,
+                                      block, max_vectors, tol, inner_rtol, inner_maxiter, precond, seed, evals, evecs,
+                                      status_out, nbasis_out, inner_iters_out, ws, ws_bytes, stream, nullptr);
+}
+
+extern "C" int lapy_eigs_shift_invert_tuned(int64_t n, const int32_t* indptr, const int32_t* indices,
+                                            const double* a_vals, const double* m_vals, int m_is_diag, int64_t nnz,
+                                            int nseg, const int32_t* seg_row, double sigma, int k, int block,
+                                            int max_vectors, double tol, double inner_rtol, int inner_maxiter,
+                                            int precond, uint64_t seed, double* evals, double* evecs,
+                                            int32_t* status_out, int32_t* nbasis_out, int64_t* inner_iters_out,
+                                            void* ws, size_t ws_bytes, void* stream,
+                                            const lapy_eigs_tuning* tuning) {
+  lapy_eigs_tuning tn{0, 0.0, 0, 0, 0};
+  if (tuning) tn = *tuning;
+  if (tn.agg_target != 0 && (tn.agg_target < kAggTarget || tn.agg_target > 1024)) {
+    lapy_set_last_message("eigs: agg_target must be 0 (default) or in [%d, 1024]", kAggTarget);
+    return LAPY_ERR_INVALID;
+  }
+  if (tn.round_rtol != 0.0 && !(tn.round_rtol > 0.0 && tn.round_rtol < 1.0)) {
+    lapy_set_last_message("eigs: round_rtol must be 0 (default) or in (0, 1)");
+    return LAPY_ERR_INVALID;
+  }
+  if (tn.fold_pieces < 0 || tn.fold_aggs < 0 || tn.ctas_per_sm < 0 || tn.ctas_per_sm > 5) {
+    lapy_set_last_message("eigs: fold thresholds must be >= 0 and ctas_per_sm in [0, 5]");
+    return LAPY_ERR_INVALID;
+  }
   if (n <= 0 || !indptr || !indices || !a_vals || !m_vals || nnz <= 0 || nseg <= 0 || !seg_row || k <= 0 ||
       !eig_block_ok(block) || !evals || !evecs || !ws || !(tol > 0) || !(inner_rtol > 0) || inner_maxiter <= 0 ||
       !eig_precond_ok(precond)) {
@@ -1298,6 +1328,10 @@ extern "C" int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const in
   }
   EigPlan P;
   plan_eig(n, nnz, nseg, seg_row, k, block, max_vectors, precond, &P);
+  if (tn.agg_target) P.agg_target = tn.agg_target;
+  if (tn.fold_pieces) P.pcg.fold_pieces = tn.fold_pieces;
+  if (tn.fold_aggs) P.pcg.fold_aggs = tn.fold_aggs;
+  if (tn.ctas_per_sm) P.pcg.ctas_per_sm = tn.ctas_per_sm;
   if (ws_bytes < layout_eig(P, nullptr, nullptr)) return LAPY_ERR_WORKSPACE;
   EigPtrs e;
   layout_eig(P, (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255)), &e);
@@ -1306,7 +1340,7 @@ extern "C" int lapy_eigs_shift_invert(int64_t n, const int32_t* indptr, const in
   // 1e-4 / 1e-5 / 2e-3 / 1e-2 per round gave 107 / 101 / 95 / 101 / 99 spectra/s;
   // tighter rounds spend iterations where FP32 CG stalls, looser ones restart
   // more often)
-  const double round_rtol = 1e-3;
+  const double round_rtol = tn.round_rtol > 0.0 ? tn.round_rtol : 1e-3;
   LAPY_TRY(eigs_run(P, e, indptr, indices, a_vals, m_vals, m_is_diag, sigma, tol, inner_rtol, round_rtol,
                     inner_maxiter, seed, evals, evecs, (cudaStream_t)stream, &r));
   for (int s = 0; s < nseg; ++s) {

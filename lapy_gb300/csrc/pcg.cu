@@ -29,10 +29,7 @@ constexpr int kUnit = 32;
 constexpr int kStageWarp = 384;   // staged nonzeros per warp (values + column indices)
 constexpr int kSellShort = 8;     // SELL slices up to this width take the all-loads-first path
 constexpr int kPlanCtasPerSm = 5; // resident CTAs per SM the warp plan assumes (48 registers)
-// Partial sums are folded into per-CTA reduction slots when a segment has
-// more pieces, or coarse unknowns, than these.
-constexpr int kFoldPieces = 64;
-constexpr int kFoldAggs = 1024;
+
 
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -1650,7 +1647,7 @@ size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size
 }
 
 template <typename V, int NP, int PC, bool RU>
-static int launch_pcg(PcgArgs<V>& args, cudaStream_t stream) {
+static int launch_pcg(PcgArgs<V>& args, int ctas_per_sm, cudaStream_t stream) {
   auto kern = pcg_kernel<V, NP, PC, RU>;
   int per_sm = 0;
   LAPY_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPcgThreads, 0));
@@ -1658,7 +1655,7 @@ static int launch_pcg(PcgArgs<V>& args, cudaStream_t stream) {
     lapy_set_last_message("pcg: kernel cannot be resident (occupancy 0)");
     return LAPY_ERR_CUDA;
   }
-  per_sm = std::min(per_sm, kPlanCtasPerSm);
+  per_sm = std::max(1, std::min({per_sm, kPlanCtasPerSm, ctas_per_sm}));
   const int grid = std::max(1, std::min(per_sm * lapy_num_sms(), (args.nvw + kWarps - 1) / kWarps));
   void* kargs[] = {(void*)&args};
   LAPY_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kPcgThreads), kargs, 0, stream));
@@ -1666,13 +1663,13 @@ static int launch_pcg(PcgArgs<V>& args, cudaStream_t stream) {
 }
 
 template <typename V, int PC, bool RU = false>
-static int launch_pcg_np(PcgArgs<V>& args, int p, cudaStream_t stream) {
+static int launch_pcg_np(PcgArgs<V>& args, int p, int ctas_per_sm, cudaStream_t stream) {
   switch (p) {
-    case 1: return launch_pcg<V, 1, PC, RU>(args, stream);
-    case 2: return launch_pcg<V, 2, PC, RU>(args, stream);
-    case 4: return launch_pcg<V, 4, PC, RU>(args, stream);
-    case 8: return launch_pcg<V, 8, PC, RU>(args, stream);
-    case 16: return launch_pcg<V, 16, PC, RU>(args, stream);
+    case 1: return launch_pcg<V, 1, PC, RU>(args, ctas_per_sm, stream);
+    case 2: return launch_pcg<V, 2, PC, RU>(args, ctas_per_sm, stream);
+    case 4: return launch_pcg<V, 4, PC, RU>(args, ctas_per_sm, stream);
+    case 8: return launch_pcg<V, 8, PC, RU>(args, ctas_per_sm, stream);
+    case 16: return launch_pcg<V, 16, PC, RU>(args, ctas_per_sm, stream);
     default:
       lapy_set_last_message("pcg: block width %d not in {1,2,4,8,16}", p);
       return LAPY_ERR_INVALID;
@@ -1685,7 +1682,8 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
                    const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
                    const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
                    cudaStream_t stream, int* iters_out, const double* K64, const double* B64, double* X64,
-                   double delta, int ru_every, int* updates_out) {
+                   double delta, int ru_every, int* updates_out, const PcgTuning* tuning) {
+  const PcgTuning tn = tuning ? *tuning : PcgTuning();
   if (ws_bytes < pcg_workspace_bytes(n, p, ct, sizeof(V), pc.kind, pc.nagg)) return LAPY_ERR_WORKSPACE;
   const bool ru = B64 != nullptr;
   char* w = (char*)(((uintptr_t)ws + 255) & ~uintptr_t(255));
@@ -1713,7 +1711,7 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
     // coarse unknowns): with few, the direct sums are cheaper
     int maxp = 0;
     for (int s = 0; s < ct.nseg; ++s) maxp = std::max(maxp, ct.h_seg_piece[s + 1] - ct.h_seg_piece[s]);
-    a.fold = (maxp > kFoldPieces || (pc.kind == kPrecTwoLevel && pc.max_seg_agg > kFoldAggs)) ? 1 : 0;
+    a.fold = (maxp > tn.fold_pieces || (pc.kind == kPrecTwoLevel && pc.max_seg_agg > tn.fold_aggs)) ? 1 : 0;
   }
   a.nvw = ct.nvw;
   a.npiece = ct.npiece;
@@ -1799,29 +1797,29 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
         lapy_set_last_message("pcg: reliable updates need the Jacobi preconditioner");
         return LAPY_ERR_INVALID;
       }
-      st = launch_pcg_np<V, kPrecJacobi, true>(a, p, stream);
+      st = launch_pcg_np<V, kPrecJacobi, true>(a, p, tn.ctas_per_sm, stream);
     } else {
       lapy_set_last_message("pcg: reliable updates run FP32 iterations");
       return LAPY_ERR_INVALID;
     }
   } else if (pc.kind == kPrecFactored) {
-    st = launch_pcg_np<V, kPrecFactored>(a, p, stream);
+    st = launch_pcg_np<V, kPrecFactored>(a, p, tn.ctas_per_sm, stream);
   } else if (pc.kind == kPrecIC0) {
     if constexpr (sizeof(V) == 4) {
-      st = launch_pcg_np<V, kPrecIC0>(a, p, stream);
+      st = launch_pcg_np<V, kPrecIC0>(a, p, tn.ctas_per_sm, stream);
     } else {
       lapy_set_last_message("pcg: the IC(0) preconditioner runs FP32 iterations");
       return LAPY_ERR_INVALID;
     }
   } else if (pc.kind == kPrecTwoLevel) {
     if constexpr (sizeof(V) == 4) {
-      st = launch_pcg_np<V, kPrecTwoLevel>(a, p, stream);
+      st = launch_pcg_np<V, kPrecTwoLevel>(a, p, tn.ctas_per_sm, stream);
     } else {
       lapy_set_last_message("pcg: the two-level preconditioner runs FP32 iterations");
       return LAPY_ERR_INVALID;
     }
   } else {
-    st = launch_pcg_np<V, kPrecJacobi>(a, p, stream);
+    st = launch_pcg_np<V, kPrecJacobi>(a, p, tn.ctas_per_sm, stream);
   }
   if (st != LAPY_OK) return st;
   if (prof) LAPY_CUDA_TRY(cudaEventRecord(e1, stream));
@@ -1861,9 +1859,9 @@ template <typename V>
 int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals,
               const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
               const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
-              cudaStream_t stream, int* iters_out) {
+              cudaStream_t stream, int* iters_out, const PcgTuning* tuning) {
   return pcg_run<V>(n, indptr, indices, vals, sell, pc, p, ct, B, X, rtol, maxiter, state_dev, ws, ws_bytes,
-                    stream, iters_out, nullptr, nullptr, nullptr, 0.0, 1, nullptr);
+                    stream, iters_out, nullptr, nullptr, nullptr, 0.0, 1, nullptr, tuning);
 }
 
 int pcg_solve_ru(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k64, const float* k32,
@@ -1874,15 +1872,17 @@ int pcg_solve_ru(int64_t n, const int32_t* indptr, const int32_t* indices, const
   pc.kind = kPrecJacobi;
   pc.dinv = dinv32;
   return pcg_run<float>(n, indptr, indices, k32, sell, pc, p, ct, nullptr, X32, rtol, maxiter, state_dev, ws,
-                        ws_bytes, stream, iters_out, k64, B, X, delta, ru_every, updates_out);
+                        ws_bytes, stream, iters_out, k64, B, X, delta, ru_every, updates_out, nullptr);
 }
 
 template int pcg_solve<float>(int64_t, const int32_t*, const int32_t*, const float*, const SellMatrix<float>*,
                               const PcgPrecondDesc<float>&, int, const ChunkTable&, const float*,
-                              float*, double, int, int32_t*, void*, size_t, cudaStream_t, int*);
+                              float*, double, int, int32_t*, void*, size_t, cudaStream_t, int*,
+                              const PcgTuning*);
 template int pcg_solve<double>(int64_t, const int32_t*, const int32_t*, const double*, const SellMatrix<double>*,
                                const PcgPrecondDesc<double>&, int, const ChunkTable&, const double*,
-                               double*, double, int, int32_t*, void*, size_t, cudaStream_t, int*);
+                               double*, double, int, int32_t*, void*, size_t, cudaStream_t, int*,
+                               const PcgTuning*);
 
 }  // namespace lapy
 

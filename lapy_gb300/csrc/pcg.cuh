@@ -142,6 +142,17 @@ struct PcgPrecondDesc {
   const int32_t* seg_avc0 = nullptr;   // nseg
 };
 
+// Launch-level knobs of the persistent PCG (autotuned per device and batch
+// shape; the defaults are the measured choice for batched mesh spectra).
+// fold_pieces / fold_aggs: fold partial sums into per-CTA reduction slots
+// when a segment has more pieces / coarse unknowns than this; ctas_per_sm:
+// resident CTAs per SM to launch (1 .. 5, the kernel's register budget).
+struct PcgTuning {
+  int fold_pieces = 64;
+  int fold_aggs = 1024;
+  int ctas_per_sm = 5;
+};
+
 // Scratch needed by one persistent PCG solve of n rows x p columns (nagg:
 // coarse unknowns of the two-level preconditioner, 0 otherwise).
 size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size, int precond, int64_t nagg = 0);
@@ -156,7 +167,7 @@ template <typename V>
 int pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals,
               const SellMatrix<V>* sell, const PcgPrecondDesc<V>& pc, int p, const ChunkTable& ct,
               const V* B, V* X, double rtol, int maxiter, int32_t* state_dev, void* ws, size_t ws_bytes,
-              cudaStream_t stream, int* iters_out);
+              cudaStream_t stream, int* iters_out, const PcgTuning* tuning = nullptr);
 
 // Mixed-precision PCG with reliable updates: FP32 Jacobi-PCG iterations
 // (k32 / sell) whose correction is folded into the FP64 solution X, and

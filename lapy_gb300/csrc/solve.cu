@@ -79,7 +79,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
     pc.kind = kPrecJacobi;
     pc.dinv = K.dinv64;
     LAPY_TRY(pcg_solve<double>(n, K.indptr, K.indices, K.k64, nullptr, pc, p, ct, B, X, rtol, maxiter, st, pws,
-                               pws_bytes, stream, &it));
+                               pws_bytes, stream, &it, &K.tuning));
     local.rounds = 1;
     local.pcg_iters = it;
     LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));
@@ -132,7 +132,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
       PcgPrecondDesc<float> pc = K.pc32;
       if (pc.kind == kPrecJacobi || pc.kind == kPrecTwoLevel) pc.dinv = K.dinv32;
       LAPY_TRY(pcg_solve<float>(n, K.indptr, K.indices, K.k32, K.sell32.val ? &K.sell32 : nullptr, pc, p, ct, R32,
-                                D32, round_rtol, maxiter, st, pws, pws_bytes, stream, &it));
+                                D32, round_rtol, maxiter, st, pws, pws_bytes, stream, &it, &K.tuning));
       local.rounds++;
       local.pcg_iters += it;
       LAPY_TRY(add_f32_to_f64(n * p, D32, X, stream));

@@ -22,6 +22,7 @@ struct SysMatrix {
   // across residual replacements stagnates on some right-hand sides (FP32
   // iterates), so the restarted rounds are the default.
   bool reliable = false;
+  PcgTuning tuning;            // launch knobs of the persistent PCG
 };
 
 struct IrStats {

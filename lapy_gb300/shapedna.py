@@ -146,10 +146,21 @@ class BatchedFEM:
 
 
 def compute_shapedna_batch(meshes, k: int = 50, lump: bool = False, block: int = 2,
-                           return_vectors: bool = True, **kw) -> list[dict]:
-    """ShapeDNA of many meshes in one batched shift-invert Lanczos solve."""
+                           return_vectors: bool = True, tuning: dict | str | None = None, **kw) -> list[dict]:
+    """ShapeDNA of many meshes in one batched shift-invert Lanczos solve.
+
+    ``tuning``: solver knobs (see ``lapy_gb300.autotune``), or ``"auto"`` for
+    the choice cached for this batch's shape class on this device (the
+    defaults when none was calibrated; the block width then comes from the
+    choice too)."""
+    if tuning == "auto":
+        from . import autotune
+
+        choice = autotune.choice_for(meshes, k)
+        block = int(choice["block"])
+        tuning = autotune.solver_tuning(choice)
     batch = BatchedFEM(meshes, lump=lump)
-    evals, evecs, info = batch.eigs(k=k, block=block, **kw)
+    evals, evecs, info = batch.eigs(k=k, block=block, tuning=tuning, **kw)
     bad = [int(s) for s in info["status"] if s != 0]
     if bad:
         _lib.check(bad[0], "compute_shapedna_batch")

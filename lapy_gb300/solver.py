@@ -252,9 +252,13 @@ class Solver:
 
 def eigs_batched(indptr, indices, a_vals, m_vals, m_is_diag: bool, seg_row, k: int, sigma: float = -0.01,
                  block: int = DEFAULT_BLOCK, tol: float = 1e-8, inner_rtol: float = 1e-9, inner_maxiter: int = 20000,
-                 max_vectors: int | None = None, seed: int = 1234, precond: str = "twolevel"):
+                 max_vectors: int | None = None, seed: int = 1234, precond: str = "twolevel",
+                 tuning: dict | None = None):
     """Shift-invert eigenpairs of every segment of a block-diagonal batch.
 
+    ``tuning``: solver knobs (``agg_target``, ``round_rtol``, ``fold_pieces``,
+    ``fold_aggs``, ``ctas_per_sm``; missing keys keep the defaults), e.g. the
+    choice of ``lapy_gb300.autotune``.
     Returns (evals: nseg x k tensor, evecs: n x k tensor, info dict)."""
     L = _lib.lib()
     pc = {"jacobi": _lib.PRECOND_JACOBI, "twolevel": _lib.PRECOND_TWO_LEVEL}.get(precond)
@@ -273,11 +277,16 @@ def eigs_batched(indptr, indices, a_vals, m_vals, m_is_diag: bool, seg_row, k: i
     status = np.zeros(nseg, dtype=np.int32)
     nbasis = np.zeros(nseg, dtype=np.int32)
     iters = C.c_int64(0)
-    _lib.check(L.lapy_eigs_shift_invert(n, dptr(indptr), dptr(indices), dptr(a_vals), dptr(m_vals), int(m_is_diag),
-                                        nnz, nseg, seg_row.ctypes.data, sigma, k, block, max_vectors, tol, inner_rtol,
-                                        inner_maxiter, pc, seed, dptr(evals), dptr(evecs), status.ctypes.data,
-                                        nbasis.ctypes.data, C.byref(iters), dptr(ws), ws.numel(), stream()),
-               "eigs_shift_invert")
+    tn = _lib.EigsTuning()
+    for key, val in (tuning or {}).items():
+        if key not in ("agg_target", "round_rtol", "fold_pieces", "fold_aggs", "ctas_per_sm"):
+            raise ValueError(f"unknown tuning key {key!r}")
+        setattr(tn, key, val)
+    _lib.check(L.lapy_eigs_shift_invert_tuned(n, dptr(indptr), dptr(indices), dptr(a_vals), dptr(m_vals),
+                                              int(m_is_diag), nnz, nseg, seg_row.ctypes.data, sigma, k, block,
+                                              max_vectors, tol, inner_rtol, inner_maxiter, pc, seed, dptr(evals),
+                                              dptr(evecs), status.ctypes.data, nbasis.ctypes.data, C.byref(iters),
+                                              dptr(ws), ws.numel(), stream(), C.byref(tn)), "eigs_shift_invert")
     info = {"status": status, "nbasis": nbasis, "inner_iters": int(iters.value), "block": block, "precond": precond,
-            "workspace_bytes": int(ws_bytes)}
+            "workspace_bytes": int(ws_bytes), "tuning": dict(tuning or {})}
     return evals, evecs, info
