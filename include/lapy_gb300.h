@@ -242,6 +242,23 @@ int lapy_pcg_solve_static(int64_t n, const int32_t* indptr, const int32_t* indic
                           int mixed, double inner_rtol, int32_t* status_out,
                           double* relres_out, int64_t* iters_out, void* stream);
 
+/* ---- curvature frame (anisotropic Laplace-Beltrami pre-step) -------------
+ * Replaces TriaMesh.curvature / curvature_tria (lapy/tria_mesh.py:1078-1279)
+ * and, through them, the host work of Solver(mesh, aniso=...)
+ * (lapy/solver.py:72-91).  v: n x 3 f64, t: m x 3 int32 (oriented), the
+ * mesh's CSR pattern (indptr, indices: diagonal and edges, as the symbolic
+ * assembly builds it), `smoothit` Laplace smoothing steps of the vertex
+ * tensors.  Outputs (device, either may be NULL), planar f64 blocks:
+ *   vtx_out (13 n): u_min (n x 3), u_max (n x 3), c_min, c_max, c_mean,
+ *                   c_gauss (n each), normals (n x 3)
+ *   tri_out (8 m):  u1 (m x 3), u2 (m x 3), c_min, c_max (m each)
+ * A mesh that is not oriented returns LAPY_ERR_INVALID with the reference's
+ * message; an element edge missing from the pattern LAPY_ERR_PATTERN. */
+size_t lapy_tria_curvature_workspace_bytes(int64_t n, int64_t m, int64_t nnz);
+int lapy_tria_curvature(const double* v, int64_t n, const int32_t* t, int64_t m, const int32_t* indptr,
+                        const int32_t* indices, int64_t nnz, int smoothit, double* vtx_out, double* tri_out,
+                        void* work, size_t ws_bytes, void* stream);
+
 /* ---- incomplete Cholesky IC(0) -------------------------------------------
  * No counterpart in the reference, which factors exactly (splu of A - sigma
  * M at lapy/solver.py:707-712, of M + t A at lapy/heat.py:226): IC(0) is the

@@ -162,7 +162,8 @@ def assemble(md: MeshDevice, pat: FemPattern, lump: bool, out_dtype=torch.float6
         st = L.lapy_fem_tria_numeric(dptr(md.v), md.coords_f32, dptr(md.t), md.m, *common)
         where = "fem_tria_numeric"
     else:
-        u1, u2, am = (torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to("cuda") for x in aniso)
+        u1, u2, am = (x.contiguous() if isinstance(x, torch.Tensor)
+                      else torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to("cuda") for x in aniso)
         st = L.lapy_fem_tria_aniso_numeric(dptr(md.v), md.coords_f32, dptr(md.t), md.m, dptr(u1), dptr(u2),
                                            dptr(am), *common)
         where = "fem_tria_aniso_numeric"
@@ -339,3 +340,20 @@ def ic0_apply(indptr, indices, l_vals, n, nnz, r: torch.Tensor, work: torch.Tens
     _lib.check(L.lapy_ic0_apply(n, dptr(indptr), dptr(indices), dptr(l_vals), nnz, R.shape[1], dptr(R), dptr(Z),
                                 dptr(work), work.numel(), stream()), "ic0_apply")
     return Z[:, 0] if r.dim() == 1 else Z
+
+
+def tria_curvature(md: MeshDevice, pat: FemPattern, smoothit: int, vertex: bool = True, triangle: bool = True):
+    """Curvature frame of a triangle mesh on the device (lapy/tria_mesh.py:
+    1078-1279): (vertex block 13 n or None, triangle block 8 m or None),
+    planar f64 blocks as include/lapy_gb300.h describes."""
+    L = _lib.lib()
+    v = md.v if md.v.dtype == torch.float64 else md.v.double()
+    vtx = torch.empty(13 * md.n, dtype=torch.float64, device="cuda") if vertex else None
+    tri = torch.empty(8 * md.m, dtype=torch.float64, device="cuda") if triangle else None
+    ws = workspace(L.lapy_tria_curvature_workspace_bytes(md.n, md.m, pat.nnz))
+    st = L.lapy_tria_curvature(dptr(v.contiguous()), md.n, dptr(md.t), md.m, dptr(pat.indptr), dptr(pat.indices),
+                               pat.nnz, int(smoothit), dptr(vtx), dptr(tri), dptr(ws), ws.numel(), stream())
+    if st == _lib.ERR_INVALID and "oriented" in L.lapy_last_error().decode(errors="replace"):
+        raise ValueError("Error: Can only compute edge information for oriented meshes!")
+    _lib.check(st, "tria_curvature")
+    return vtx, tri

@@ -108,6 +108,8 @@ _SIGNATURES = {
     "lapy_spai_pcg_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int]),
     "lapy_spai_pcg_solve": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _dbl, _int, _dbl, _vp, _vp,
                                    _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(_i64), _vp, _sz, _vp]),
+    "lapy_tria_curvature_workspace_bytes": (_sz, [_i64, _i64, _i64]),
+    "lapy_tria_curvature": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _i64, _int, _vp, _vp, _vp, _sz, _vp]),
     "lapy_ic0_workspace_bytes": (_sz, [_i64, _i64, _int]),
     "lapy_ic0_factor": (_int, [_i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
     "lapy_ic0_apply": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _vp, _vp, _sz, _vp]),

@@ -36,6 +36,7 @@ EXTRA = {
     "assemble.cu": ["--fmad=false"],
     "geodesic.cu": ["--fmad=false"],
     "ic0.cu": ["--fmad=false"],
+    "curvature.cu": ["--fmad=false"],
 }
 
 

@@ -28,7 +28,7 @@ from scipy import sparse
 
 from . import _lib
 from ._device import (DeviceCSR, assemble, dptr, mesh_device, pattern_of, pcg_solve, require_cuda, stream,
-                      workspace)
+                      tria_curvature, workspace)
 
 logger = logging.getLogger(__name__)
 
@@ -58,17 +58,24 @@ class Solver:
         if gname == "TriaMesh":
             if aniso is not None:
                 logger.info("TriaMesh with anisotropic Laplace-Beltrami")
-                u1, u2, c1, c2 = geometry.curvature_tria(smoothit=aniso_smooth)
                 if isinstance(aniso, (list, tuple, set, np.ndarray)):
                     if len(aniso) != 2:
                         raise ValueError("aniso should be scalar or tuple/array of length 2!")
                     aniso0, aniso1 = list(aniso)
                 else:
                     aniso0 = aniso1 = aniso
-                aniso_mat = np.empty((geometry.t.shape[0], 2), dtype=dtype)
+                # curvature frame on the device (lapy/tria_mesh.py:1221-1279);
+                # the two curvature weights exp(-a |c|) (solver.py:88-90) are
+                # formed on the host from the m pooled curvatures
+                md, pat = pattern_of(geometry)
+                _, tri = tria_curvature(md, pat, aniso_smooth, vertex=False, triangle=True)
+                m = md.m
+                c = tri[6 * m:].cpu().numpy()
+                c1, c2 = c[:m], c[m:]
+                aniso_mat = np.empty((m, 2), dtype=dtype)
                 aniso_mat[:, 1] = np.exp(-aniso1 * np.abs(c1))
                 aniso_mat[:, 0] = np.exp(-aniso0 * np.abs(c2))
-                aniso_inputs = (u1, u2, aniso_mat)
+                aniso_inputs = (tri[:3 * m].view(m, 3), tri[3 * m:6 * m].view(m, 3), aniso_mat)
             else:
                 logger.info("TriaMesh with regular Laplace-Beltrami")
         elif gname == "TetMesh":

@@ -3,10 +3,10 @@
 Mirrors the constructor contract of lapy/tria_mesh.py:182-280 (TriaMesh):
 vertices ``v`` (n x 3, or n x 2 padded with z = 0), triangles ``t`` (m x 3),
 the same validation errors.  Geometry work that lies on the FEM path
-(``avg_edge_length``) runs on the GPU; ``refine_`` (host-side mesh
-construction), the measures used by spectra normalisation, the text file
-formats and the curvature pre-step of the anisotropic Laplacian
-(``curvature_tria``) live in NumPy, as inputs to the GPU kernels.
+(``avg_edge_length`` and the curvature frame of the anisotropic Laplacian,
+``curvature`` / ``curvature_tria``) runs on the GPU; ``refine_`` (host-side
+mesh construction), the measures used by spectra normalisation and the text
+file formats live in NumPy.
 """
 
 from __future__ import annotations
@@ -184,19 +184,28 @@ class TriaMesh:
 
     def curvature(self, smoothit: int = 3):
         """Principal directions and curvatures at the vertices
-        (lapy/tria_mesh.py:1078-1219): u_min, u_max, c_min, c_max, c_mean,
-        c_gauss, normals."""
-        from . import _curvature
+        (lapy/tria_mesh.py:1078-1219), computed on the GPU: u_min, u_max,
+        c_min, c_max, c_mean, c_gauss, normals."""
+        from ._device import pattern_of, tria_curvature
 
-        return _curvature.curvature(self.v, self.t, smoothit)
+        md, pat = pattern_of(self)
+        vtx, _ = tria_curvature(md, pat, smoothit, vertex=True, triangle=False)
+        b = vtx.cpu().numpy()
+        n = md.n
+        return (b[:3 * n].reshape(n, 3), b[3 * n:6 * n].reshape(n, 3), b[6 * n:7 * n], b[7 * n:8 * n],
+                b[8 * n:9 * n], b[9 * n:10 * n], b[10 * n:].reshape(n, 3))
 
     def curvature_tria(self, smoothit: int = 3):
         """Principal directions and curvatures on the triangles, the frame of
-        the anisotropic Laplace-Beltrami assembly (lapy/tria_mesh.py:1221-1279):
-        u_min, u_max, c_min, c_max."""
-        from . import _curvature
+        the anisotropic Laplace-Beltrami assembly (lapy/tria_mesh.py:1221-1279),
+        computed on the GPU: u_min, u_max, c_min, c_max."""
+        from ._device import pattern_of, tria_curvature
 
-        return _curvature.curvature_tria(self.v, self.t, smoothit)
+        md, pat = pattern_of(self)
+        _, tri = tria_curvature(md, pat, smoothit, vertex=False, triangle=True)
+        b = tri.cpu().numpy()
+        m = md.m
+        return b[:3 * m].reshape(m, 3), b[3 * m:6 * m].reshape(m, 3), b[6 * m:7 * m], b[7 * m:]
 
     def centroid(self) -> tuple[np.ndarray, float]:
         """Area-weighted mean of the triangle centres, and the total area
