@@ -42,6 +42,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "k=50 spectra/s (batched ShapeDNA, eig rel err <= 1e-8)"
+# ncu dram__bytes_read.sum + dram__bytes_write.sum per pcg_kernel launch of the 512-mesh step
+PCG_TRAFFIC_PER_LAUNCH = 9.175e12 / 147
 K_EIG = 50
 
 
@@ -350,7 +352,13 @@ def run_gpu(args, rank, world):
                  "d2h_bytes_per_step": d2h, "calls": e2e_steps} if e2e_steps else None),
         "roofline": {"bound": "hbm", "kernel": "pcg_kernel (persistent FP32 two-level PCG)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "frac": (achieved / hbm) if achieved else None,
+                     # DRAM bytes per pcg_kernel launch, from one ncu pass over a full-size step
+                     # (profiles/pcg_kernel_traffic_batched_shapedna_512.md): 1.10x the algorithmic bytes
+                     "traffic": PCG_TRAFFIC_PER_LAUNCH if args.meshes == 512 else None,
+                     "traffic_unit": "bytes per launch",
+                     "algorithmic_per_launch": (prof["algorithmic_bytes"] / prof["pcg_launches"]
+                                                if prof["pcg_launches"] else None),
                      "peak_kind": f"{peak_kind} hbm_gbs",
                      "pcg_share_of_step": prof["pcg_ms"] / 1e3 / dev_s if dev_s > 0 else None},
         "gpu_launches": int(launches),
