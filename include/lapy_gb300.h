@@ -144,6 +144,26 @@ int lapy_csr_pattern_map(int64_t n, const int32_t* a_indptr, const int32_t* a_in
                          const int32_t* b_indptr, const int32_t* b_indices,
                          int64_t b_nnz, int32_t* pos, void* work, void* stream);
 
+/* Batch construction (the reference handles one mesh per call; a batch of
+ * meshes is concatenated into one block-diagonal system).
+ * lapy_h2d_concat: `count` host buffers (src[i], bytes[i]) copied back to
+ * back into the device buffer dst, in order, on `stream`.
+ * lapy_seg_offset_elements: t_out (device, m x npe int32) = t_in (device, the
+ * meshes' own vertex indices concatenated; int64 if idx64 else int32) +
+ * seg_row[s] for the elements [seg_elem[s], seg_elem[s+1]) of mesh s
+ * (seg_elem, seg_row: device, nseg+1 each).  seg_max (device, nseg+1 int32)
+ * receives each mesh's largest index, and seg_max[nseg] != 0 if an index was
+ * outside its mesh's rows.
+ * lapy_seg_unit_vector: out (device, n) = the indicator of vertex vid[s] of
+ * every mesh s (the right-hand sides of heat.diffusion, lapy/heat.py:215-221,
+ * for one seed vertex per mesh). */
+int lapy_h2d_concat(int count, const void* const* src, const size_t* bytes, void* dst, void* stream);
+int lapy_seg_offset_elements(int64_t m, int npe, int nseg, const int32_t* seg_elem,
+                             const int32_t* seg_row, const void* t_in, int idx64, int32_t* t_out,
+                             int32_t* seg_max, void* stream);
+int lapy_seg_unit_vector(int64_t n, int nseg, const int32_t* seg_row, const int32_t* vid, double* out,
+                         void* stream);
+
 /* Mean edge length over the strict upper triangle of the pattern
  * (lapy/tria_mesh.py:735-748, lapy/tet_mesh.py:182-195: the mean of
  * ||v_i - v_j|| over the distinct edges).  Result written to *out (host). */

@@ -119,3 +119,22 @@ extern "C" const char* lapy_status_string(int status) {
 }
 
 extern "C" const char* lapy_last_error(void) { return g_last_error; }
+
+// Host buffers copied back to back into one device buffer (one
+// cudaMemcpyAsync per buffer, in order).
+extern "C" int lapy_h2d_concat(int count, const void* const* src, const size_t* bytes, void* dst, void* stream) {
+  if (count < 0 || (count > 0 && (!src || !bytes || !dst))) return LAPY_ERR_INVALID;
+  size_t off = 0;
+  for (int i = 0; i < count; ++i) {
+    if (bytes[i] == 0) continue;
+    if (!src[i]) return LAPY_ERR_INVALID;
+    const cudaError_t e = cudaMemcpyAsync((char*)dst + off, src[i], bytes[i], cudaMemcpyHostToDevice,
+                                          (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+      lapy_set_last_cuda_error(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+      return LAPY_ERR_CUDA;
+    }
+    off += bytes[i];
+  }
+  return LAPY_OK;
+}

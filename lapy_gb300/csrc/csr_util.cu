@@ -220,3 +220,72 @@ extern "C" int lapy_avg_edge_length(const void* v, int coords_f32, int64_t n, co
   LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
   return LAPY_OK;
 }
+
+// ---- batch construction ------------------------------------------------------
+// Element connectivity of concatenated meshes: t_out (m x npe int32) = t_in
+// (each mesh's own vertex indices, int32 or int64) + seg_row[s] for the mesh
+// s whose element range [seg_elem[s], seg_elem[s+1]) holds the element.
+// Indices outside [0, rows of the mesh) set *bad; seg_max[s] receives the
+// largest index of mesh s (so the host can check that every vertex is used).
+template <typename I>
+__global__ void seg_offset_elements_kernel(int64_t m, int npe, int nseg, const int32_t* __restrict__ seg_elem,
+                                           const int32_t* __restrict__ seg_row, const I* __restrict__ t_in,
+                                           int32_t* __restrict__ t_out, int* __restrict__ seg_max,
+                                           int* __restrict__ bad) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m) return;
+  int lo = 0, hi = nseg - 1;  // largest s with seg_elem[s] <= e
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((int64_t)seg_elem[mid] <= e) lo = mid; else hi = mid - 1;
+  }
+  const int32_t off = seg_row[lo], rows = seg_row[lo + 1] - off;
+  int mx = -1;
+  for (int c = 0; c < npe; ++c) {
+    const I x = t_in[e * npe + c];
+    if (x < 0 || x >= (I)rows) {
+      atomicOr(bad, 1);
+      t_out[e * npe + c] = off;
+    } else {
+      t_out[e * npe + c] = off + (int32_t)x;
+      mx = max(mx, (int)x);
+    }
+  }
+  atomicMax(&seg_max[lo], mx);
+}
+
+// out[seg_row[s] + vid[s]] = 1 for every segment s (out zeroed before).
+__global__ void seg_unit_set_kernel(int nseg, const int32_t* __restrict__ seg_row, const int32_t* __restrict__ vid,
+                                    double* __restrict__ out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nseg) out[(int64_t)seg_row[s] + vid[s]] = 1.0;
+}
+
+extern "C" int lapy_seg_offset_elements(int64_t m, int npe, int nseg, const int32_t* seg_elem,
+                                        const int32_t* seg_row, const void* t_in, int idx64, int32_t* t_out,
+                                        int32_t* seg_max, void* stream) {
+  if (m < 0 || npe <= 0 || nseg <= 0 || !seg_elem || !seg_row || !seg_max || (m > 0 && (!t_in || !t_out)))
+    return LAPY_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  // seg_max[nseg] doubles as the out-of-range flag
+  LAPY_CUDA_TRY(cudaMemsetAsync(seg_max, 0xff, sizeof(int32_t) * (size_t)nseg, st));
+  LAPY_CUDA_TRY(cudaMemsetAsync(seg_max + nseg, 0, sizeof(int32_t), st));
+  if (m == 0) return LAPY_OK;
+  const unsigned nb = lapy_ceil_div(m, 256);
+  if (idx64)
+    seg_offset_elements_kernel<int64_t><<<nb, 256, 0, st>>>(m, npe, nseg, seg_elem, seg_row, (const int64_t*)t_in,
+                                                            t_out, seg_max, seg_max + nseg);
+  else
+    seg_offset_elements_kernel<int32_t><<<nb, 256, 0, st>>>(m, npe, nseg, seg_elem, seg_row, (const int32_t*)t_in,
+                                                            t_out, seg_max, seg_max + nseg);
+  return lapy_check_launch("seg_offset_elements_kernel");
+}
+
+extern "C" int lapy_seg_unit_vector(int64_t n, int nseg, const int32_t* seg_row, const int32_t* vid, double* out,
+                                    void* stream) {
+  if (n <= 0 || nseg <= 0 || !seg_row || !vid || !out) return LAPY_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  LAPY_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * (size_t)n, st));
+  seg_unit_set_kernel<<<lapy_ceil_div(nseg, 256), 256, 0, st>>>(nseg, seg_row, vid, out);
+  return lapy_check_launch("seg_unit_set_kernel");
+}

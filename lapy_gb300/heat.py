@@ -163,9 +163,10 @@ class HeatBatch:
             raise ValueError("vids needs one vertex per mesh (or one vertex for all)")
         if np.any(v < 0) or np.any(v >= sizes):
             raise ValueError("vids contains out-of-range vertex indices")
-        b0 = np.zeros(seg[-1])
-        b0[seg[:-1] + v] = 1.0
-        self.b0 = torch.from_numpy(b0).to("cuda")
+        vid = torch.from_numpy(v.astype(np.int32)).to("cuda")
+        self.b0 = torch.empty(int(seg[-1]), dtype=torch.float64, device="cuda")
+        _lib.check(_lib.lib().lapy_seg_unit_vector(int(seg[-1]), nseg, dptr(batch_input.seg_row_dev), dptr(vid),
+                                                   dptr(self.b0), stream()), "seg_unit_vector")
         self.ones = torch.ones(nseg, dtype=torch.float64, device="cuda")
 
     def solve(self, rtol: float = 1e-11, maxiter: int = 20000, precond: str = "jacobi"):

@@ -4,11 +4,13 @@ block-diagonal assembly and one batched eigensolve."""
 
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import torch
 
 from . import _lib
-from ._device import DeviceCSR, MeshDevice, assemble, build_pattern, require_cuda
+from ._device import DeviceCSR, MeshDevice, assemble, build_pattern, dptr, require_cuda, stream
 from .solver import DEFAULT_BLOCK, Solver, eigs_batched
 
 
@@ -91,29 +93,52 @@ class BatchInput:
         require_cuda()
         if not meshes:
             raise ValueError("empty batch")
-        npe = meshes[0].t.shape[1]
-        vs, ts, seg, segel = [], [], [0], [0]
+        L = _lib.lib()
+        npe = np.asarray(meshes[0].t).shape[1]
         f32 = all(np.asarray(m.v).dtype == np.float32 for m in meshes)
+        vdt = np.float32 if f32 else np.float64
+        vs, ts, seg, segel = [], [], [0], [0]
         for m in meshes:
             t = np.asarray(m.t)
-            if t.shape[1] != npe:
+            if t.ndim != 2 or t.shape[1] != npe:
                 raise ValueError("a batch holds meshes of one element type")
-            nv = len(m.v)
-            if int(t.max()) + 1 != nv:
-                raise ValueError("batched meshes must reference every vertex")
-            vs.append(np.asarray(m.v, dtype=np.float32 if f32 else np.float64))
-            ts.append(t.astype(np.int64) + seg[-1])
-            seg.append(seg[-1] + nv)
+            v = np.ascontiguousarray(m.v, dtype=vdt)
+            vs.append(v)
+            ts.append(t)
+            seg.append(seg[-1] + len(v))
             segel.append(segel[-1] + len(t))
-        if seg[-1] >= 2**31:
+        if seg[-1] >= 2**31 or segel[-1] * npe >= 2**31:
             raise ValueError("batch exceeds the int32 index range")
-        v = torch.from_numpy(np.ascontiguousarray(np.concatenate(vs))).to("cuda")
-        t = torch.from_numpy(np.ascontiguousarray(np.concatenate(ts).astype(np.int32))).to("cuda")
-        self.mesh = MeshDevice(v, t, seg[-1], seg[-1], t.shape[0], npe)
+        idx64 = not all(t.dtype == np.int32 for t in ts)
+        ts = [np.ascontiguousarray(t, dtype=np.int64 if idx64 else np.int32) for t in ts]
+        n, m_tot, nseg = seg[-1], segel[-1], len(meshes)
+        s = stream()
+
+        def upload(arrays, out):
+            ptrs = (C.c_void_p * len(arrays))(*[a.ctypes.data for a in arrays])
+            sizes = (C.c_size_t * len(arrays))(*[a.nbytes for a in arrays])
+            _lib.check(L.lapy_h2d_concat(len(arrays), ptrs, sizes, dptr(out), s), "h2d_concat")
+
+        # every mesh's arrays straight into the device buffers; the element
+        # indices are offset (and checked) on the device
+        v = torch.empty((n, 3), dtype=torch.float32 if f32 else torch.float64, device="cuda")
+        upload(vs, v)
+        traw = torch.empty((m_tot, npe), dtype=torch.int64 if idx64 else torch.int32, device="cuda")
+        upload(ts, traw)
         self.seg_row = np.array(seg, dtype=np.int32)
-        self.seg_row_dev = torch.from_numpy(self.seg_row).to("cuda")
         self.seg_elem = np.array(segel, dtype=np.int32)
+        self.seg_row_dev = torch.from_numpy(self.seg_row).to("cuda")
         self.seg_elem_dev = torch.from_numpy(self.seg_elem).to("cuda")
+        t = torch.empty((m_tot, npe), dtype=torch.int32, device="cuda")
+        segmax = torch.empty(nseg + 1, dtype=torch.int32, device="cuda")
+        _lib.check(L.lapy_seg_offset_elements(m_tot, npe, nseg, dptr(self.seg_elem_dev), dptr(self.seg_row_dev),
+                                              dptr(traw), int(idx64), dptr(t), dptr(segmax), s), "seg_offset_elements")
+        sm = segmax.cpu().numpy()
+        if sm[nseg] != 0:
+            raise ValueError("element indices outside their mesh's vertices")
+        if np.any(sm[:nseg] + 1 != np.diff(self.seg_row)):
+            raise ValueError("batched meshes must reference every vertex")
+        self.mesh = MeshDevice(v, t, n, n, m_tot, npe)
 
 
 class BatchedFEM:

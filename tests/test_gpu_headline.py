@@ -87,3 +87,26 @@ def test_batched_clamp_is_per_mesh(cuda_ok):
         # the mass carries this mesh's clamp (the oracle's mean is NumPy's)
         Mref = oracle.assemble_sorted(np.asarray(mesh.v), np.asarray(mesh.t))[1]
         np.testing.assert_allclose(m[k0:k1], Mref.data, rtol=1e-14, atol=0)
+
+
+def test_batch_input_built_on_the_device(cuda_ok):
+    """Meshes concatenated into one batch: vertex blocks stacked, element
+    indices offset on the device (int64 and int32 inputs), and the reference's
+    preconditions checked there (indices inside the mesh, every vertex used)."""
+    from lapy_gb300 import TriaMesh, meshes, shapedna
+
+    ms = [meshes.sh_deform(meshes.icosphere(2), seed=1), meshes.icosphere(1), meshes.sh_deform(meshes.icosphere(3), 2)]
+    for dt in (np.int64, np.int32):
+        batch = [TriaMesh(m.v, np.asarray(m.t, dtype=dt)) for m in ms]
+        inp = shapedna.BatchInput(batch)
+        off = np.cumsum([0] + [len(m.v) for m in ms])
+        want = np.concatenate([np.asarray(m.t) + off[i] for i, m in enumerate(ms)])
+        np.testing.assert_array_equal(inp.mesh.t.cpu().numpy(), want)
+        np.testing.assert_array_equal(inp.mesh.v.cpu().numpy(), np.concatenate([m.v for m in ms]))
+    bad = TriaMesh(ms[1].v, ms[1].t.copy())
+    bad.t[0, 0] = len(bad.v)  # outside the mesh
+    with pytest.raises(ValueError, match="outside"):
+        shapedna.BatchInput([ms[0], bad])
+    extra = TriaMesh(np.vstack([ms[1].v, [[0.0, 0.0, 2.0]]]), ms[1].t)  # a vertex no triangle uses
+    with pytest.raises(ValueError, match="every vertex"):
+        shapedna.BatchInput([ms[0], extra])
