@@ -2,7 +2,8 @@
 //
 // For an SPD system K on a symmetric mesh pattern, G is lower triangular on
 // the pattern's lower part.  A per-edge network (6 -> 64 -> 64 -> 1, tanh,
-// BF16 weights, FP32 arithmetic) emits w_ij for every strictly lower entry;
+// BF16 weights, FP32 accumulation; the forward pass's 64 x 64 layer on the
+// tensor pipe) emits w_ij for every strictly lower entry;
 // row i then gets
 //   q_i = (e_i - w_i)' K (e_i - w_i),  G_ii = q_i^-1/2,  G_ij = -w_ij G_ii,
 // so diag(G K G') = 1 and G'G is SPD for every w (w = 0 is Jacobi).  The
@@ -160,21 +161,125 @@ __device__ __forceinline__ float layer2_unit(const SpaiWeights& s, const float (
   return (a0 + a1) + (a2 + a3);
 }
 
-__global__ void __launch_bounds__(128) spai_forward_kernel(int64_t ne, const float* __restrict__ feat,
-                                                           const __nv_bfloat16* __restrict__ wb,
-                                                           float* __restrict__ out) {
-  __shared__ __align__(16) SpaiWeights s;
-  load_weights(wb, s);
+// ---- network on the tensor pipe ---------------------------------------------
+// Forward pass with warp-level BF16 matrix instructions
+// (mma.sync.m16n8k16, FP32 accumulate): a warp takes 16 edges at a time.
+// Layer 1 (6 -> 64) runs on the FP32 pipe, each lane computing exactly the
+// hidden units its A fragments hold (rows lane/4 and lane/4 + 8, units
+// 16t + 2(lane%4) + {0,1} and + 8 of every 16-unit step t), so no shuffles
+// are needed.  Layer 2 (64 x 64, 90 % of the work) is 32 tiles of 16 x 8 x 16
+// per 16 edges; its input is split into three BF16 terms (hi + mid + lo,
+// about 24 bits) so that the product with the BF16 weights keeps the FP32
+// path's accuracy.  Layer 3 (64 -> 1) is folded into the epilogue of each
+// 8-unit output tile, and the four lanes of a row sum their parts.
+constexpr int kMmaWarps = 4;
+constexpr int kW2Ld = kHid + 8;  // padded row of the staged W2 (BF16): conflict-free B-fragment loads
+
+struct SpaiMmaSmem {
+  __nv_bfloat16 W2[kHid * kW2Ld];
+  float W1[kHid * kNF], b1[kHid], b2[kHid], W3[kHid], b3;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const uint32_t l = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
+  const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
+  return l | (h << 16);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__global__ void __launch_bounds__(32 * kMmaWarps) spai_forward_mma_kernel(int64_t ne, const float* __restrict__ feat,
+                                                                          const __nv_bfloat16* __restrict__ wb,
+                                                                          float* __restrict__ out) {
+  __shared__ __align__(16) SpaiMmaSmem s;
+  for (int p = threadIdx.x; p < kHid * kHid; p += blockDim.x) s.W2[(p / kHid) * kW2Ld + p % kHid] = wb[kOW2 + p];
+  for (int p = threadIdx.x; p < kHid * kNF; p += blockDim.x) s.W1[p] = __bfloat162float(wb[kOW1 + p]);
+  for (int p = threadIdx.x; p < kHid; p += blockDim.x) {
+    s.b1[p] = __bfloat162float(wb[kOB1 + p]);
+    s.b2[p] = __bfloat162float(wb[kOB2 + p]);
+    s.W3[p] = __bfloat162float(wb[kOW3 + p]);
+  }
+  if (threadIdx.x == 0) s.b3 = __bfloat162float(wb[kOB3]);
   __syncthreads();
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
-    float f[kNF], h1[kHid];
+  const int lane = threadIdx.x & 31, grp = lane >> 2, tig = lane & 3;
+  const int64_t warp0 = (int64_t)blockIdx.x * kMmaWarps + (threadIdx.x >> 5);
+  const int64_t nwarp = (int64_t)gridDim.x * kMmaWarps;
+  const uint32_t* W2w = reinterpret_cast<const uint32_t*>(s.W2);  // two BF16 per word
+  for (int64_t tile = warp0; tile * 16 < ne; tile += nwarp) {
+    const int64_t e0 = tile * 16 + grp, e1 = e0 + 8;
+    float f0[kNF], f1[kNF];
 #pragma unroll
-    for (int k = 0; k < kNF; ++k) f[k] = feat[e * kNF + k];
-    layer1(s, f, h1);
-    float w = s.b3;
-#pragma unroll 1
-    for (int o = 0; o < kHid; ++o) w = fmaf(s.W3[o], tanhf(layer2_unit(s, h1, o)), w);
-    out[e] = w;
+    for (int k = 0; k < kNF; ++k) {
+      f0[k] = e0 < ne ? feat[e0 * kNF + k] : 0.f;
+      f1[k] = e1 < ne ? feat[e1 * kNF + k] : 0.f;
+    }
+    // layer 1 for this lane's fragment units; A fragments of layer 2 in
+    // three BF16 terms
+    uint32_t ahi[4][4], amid[4][4], alo[4][4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {  // units 16t + 8 half + 2 tig + {0, 1}
+        const int u = 16 * t + 8 * half + 2 * tig;
+        float h[2][2];  // [row 0/8][unit u/u+1]
+#pragma unroll
+        for (int du = 0; du < 2; ++du) {
+          float a0 = s.b1[u + du], a1 = s.b1[u + du];
+#pragma unroll
+          for (int k = 0; k < kNF; ++k) {
+            a0 = fmaf(s.W1[(u + du) * kNF + k], f0[k], a0);
+            a1 = fmaf(s.W1[(u + du) * kNF + k], f1[k], a1);
+          }
+          h[0][du] = tanhf(a0);
+          h[1][du] = tanhf(a1);
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const int reg = 2 * half + r;  // a0: (row, k), a1: (row + 8, k), a2: (row, k + 8), a3: (row + 8, k + 8)
+          float x0 = h[r][0], x1 = h[r][1];
+          const float hi0 = __bfloat162float(__float2bfloat16_rn(x0)), hi1 = __bfloat162float(__float2bfloat16_rn(x1));
+          ahi[t][reg] = pack_bf16x2(x0, x1);
+          x0 -= hi0;
+          x1 -= hi1;
+          const float mi0 = __bfloat162float(__float2bfloat16_rn(x0)), mi1 = __bfloat162float(__float2bfloat16_rn(x1));
+          amid[t][reg] = pack_bf16x2(x0, x1);
+          alo[t][reg] = pack_bf16x2(x0 - mi0, x1 - mi1);
+        }
+      }
+    }
+    float part0 = 0.f, part1 = 0.f;  // layer-3 partial sums of rows grp and grp + 8
+#pragma unroll 2
+    for (int j = 0; j < kHid / 8; ++j) {  // output units 8j .. 8j + 7
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      const int n = 8 * j + grp;  // B column = W2 row
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const uint32_t b0 = W2w[(n * kW2Ld + 16 * t + 2 * tig) >> 1];
+        const uint32_t b1 = W2w[(n * kW2Ld + 16 * t + 8 + 2 * tig) >> 1];
+        mma_bf16_16816(acc, alo[t], b0, b1);
+        mma_bf16_16816(acc, amid[t], b0, b1);
+        mma_bf16_16816(acc, ahi[t], b0, b1);
+      }
+      const int o = 8 * j + 2 * tig;
+      part0 = fmaf(s.W3[o], tanhf(acc[0] + s.b2[o]), part0);
+      part0 = fmaf(s.W3[o + 1], tanhf(acc[1] + s.b2[o + 1]), part0);
+      part1 = fmaf(s.W3[o], tanhf(acc[2] + s.b2[o]), part1);
+      part1 = fmaf(s.W3[o + 1], tanhf(acc[3] + s.b2[o + 1]), part1);
+    }
+    part0 += __shfl_xor_sync(0xffffffffu, part0, 1);
+    part0 += __shfl_xor_sync(0xffffffffu, part0, 2);
+    part1 += __shfl_xor_sync(0xffffffffu, part1, 1);
+    part1 += __shfl_xor_sync(0xffffffffu, part1, 2);
+    if (tig == 0) {
+      if (e0 < ne) out[e0] = s.b3 + part0;
+      if (e1 < ne) out[e1] = s.b3 + part1;
+    }
   }
 }
 
@@ -443,9 +548,10 @@ extern "C" int lapy_spai_features(int64_t n, int nseg, const int32_t* seg_row, c
 extern "C" int lapy_spai_forward(int64_t ne, const float* feat, const void* weights_bf16, float* w_out,
                                  void* stream_) {
   if (ne <= 0 || !feat || !weights_bf16 || !w_out) return LAPY_ERR_INVALID;
-  const unsigned grid = std::min<unsigned>(lapy_ceil_div(ne, 128), 16u * lapy_num_sms());
-  spai_forward_kernel<<<grid, 128, 0, (cudaStream_t)stream_>>>(ne, feat, (const __nv_bfloat16*)weights_bf16, w_out);
-  return lapy_check_launch("spai_forward_kernel");
+  const unsigned grid = std::min<unsigned>(lapy_ceil_div(ne, 16 * kMmaWarps), 16u * lapy_num_sms());
+  spai_forward_mma_kernel<<<grid, 32 * kMmaWarps, 0, (cudaStream_t)stream_>>>(
+      ne, feat, (const __nv_bfloat16*)weights_bf16, w_out);
+  return lapy_check_launch("spai_forward_mma_kernel");
 }
 
 extern "C" int lapy_spai_factor(int64_t n, const int32_t* indptr, const int32_t* indices, const double* k_vals,
