@@ -52,7 +52,7 @@ void lapy_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 bool lapy_profile_enabled() { return g_prof_on; }
 
 void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int eb, int precond,
-                          double coarse_bytes) {
+                          double coarse_bytes, bool restrict_fused) {
   std::lock_guard<std::mutex> lock(g_prof_mu);
   g_prof[0] += ms;
   g_prof[1] += 1;
@@ -65,8 +65,12 @@ void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long 
   // two-level (precond 2): 12 vector streams (SpMM: P in, Q out; update: X,
   // P, Q, R in, X, R out; restriction: R in; direction: R, P in, P out), 2 of
   // the diagonal, the aggregate index per row, and the BF16 coarse inverse
-  // the coarse solves streamed
-  if (precond == 2)
+  // the coarse solves streamed.  With the restriction fused into the update
+  // (aggregates are row ranges) it reads no R of its own: 11 vector streams
+  // and the aggregate index twice (update, direction).
+  if (precond == 2 && restrict_fused)
+    g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (11.0 * p * eb + 2.0 * eb + 8.0) + coarse_bytes;
+  else if (precond == 2)
     g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (12.0 * p * eb + 2.0 * eb + 4.0) + coarse_bytes;
   else
     g_prof[5] += (double)nnz * (eb + 4) + (double)rows * (4 + 11.0 * p * eb + 2.0 * eb);

@@ -29,7 +29,7 @@ void lapy_count_launch();
 // PCG profile accumulation (enabled by lapy_profile_enable).
 bool lapy_profile_enabled();
 void lapy_profile_add_pcg(double ms, long long iters, long long rows, long long nnz, int p, int elem_bytes,
-                          int precond, double coarse_bytes);
+                          int precond, double coarse_bytes, bool restrict_fused);
 void lapy_profile_add_reorth(long long steps, long long second_passes);
 // Per-phase device time of the persistent PCG (profile mode): the interval
 // between consecutive grid-barrier exits, accumulated per phase: initialisation,

@@ -199,6 +199,8 @@ struct PcgArgs {
   S* rc;              // [nagg][NP] restricted residual W'r   (two-level)
   S* yc;              // [nagg][NP] coarse solution (W'KW)^-1 W'r
   S* csl;             // [nagg][NP] rc .* yc (coarse part of r'z)
+  S* rc_part;         // [2][npiece][NP] partial rc of aggregates that straddle pieces
+  int32_t* rc_cnt;    // [nagg] arrivals at a straddling aggregate (zero between phases)
   S* rz;              // [2][nseg][NP]
   S* bb;              // [nseg][NP]
   int32_t* state;     // [2][nseg][NP]
@@ -660,6 +662,55 @@ __device__ __forceinline__ void coarse_restrict(const PcgArgs<V>& a, const int32
       if (lane == q) a.rc[(int64_t)g * NP + q] = v;
     }
   })
+}
+
+// Restriction fused into the update phase (aggregates are contiguous row
+// ranges): piece p has summed its rows of aggregate g into acc (per lane).
+// An aggregate inside the piece's rows is written to rc directly.  One that
+// straddles pieces pa..pb leaves one partial per piece: the piece it starts in
+// writes its tail slot (2 pa + 1), every later piece its head slot (2 p); the
+// last of them to arrive (a counter per aggregate) sums the partials in piece
+// order, so the result does not depend on the arrival order, writes rc and
+// clears the counter.  head / tail: g is the piece's first aggregate and
+// began in an earlier piece / its last one and goes on in a later piece.
+// Called by the whole warp.
+template <typename V, int NP, typename S>
+__device__ __forceinline__ void restrict_flush(const PcgArgs<V>& a, int p, int g, bool head, bool tail,
+                                               const S (&acc)[NP]) {
+  const int lane = threadIdx.x & 31;
+  S tot[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) tot[q] = warp_sum(acc[q]);
+  if (!head && !tail) {
+#pragma unroll
+    for (int q = 0; q < NP; ++q)
+      if (lane == q) a.rc[(int64_t)g * NP + q] = tot[q];
+    return;
+  }
+  const int slot = 2 * p + (head ? 0 : 1);
+#pragma unroll
+  for (int q = 0; q < NP; ++q)
+    if (lane == q) a.rc_part[(int64_t)slot * NP + q] = tot[q];
+  __threadfence();
+  __syncwarp();
+  int pa = p, pb = p, last = 0;
+  if (lane == 0) {
+    const int ga = a.pc.agg_ptr[g], gb = a.pc.agg_ptr[g + 1];
+    while (a.unit_row[a.piece_unit[pa]] > ga) --pa;
+    while (a.unit_row[a.piece_unit[pb + 1]] < gb) ++pb;
+    last = atomicAdd(a.rc_cnt + g, 1) == pb - pa;
+  }
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (!last) return;
+  pa = __shfl_sync(0xffffffffu, pa, 0);
+  pb = __shfl_sync(0xffffffffu, pb, 0);
+  __threadfence();
+  if (lane < NP) {
+    S sum = S(0);
+    for (int pp = pa; pp <= pb; ++pp) sum += __ldcg(a.rc_part + (int64_t)(2 * pp + (pp == pa ? 1 : 0)) * NP + lane);
+    a.rc[(int64_t)g * NP + lane] = sum;
+  }
+  if (lane == 0) a.rc_cnt[g] = 0;
 }
 
 // BF16 element e (0..3) of four packed in a uint2 (element 0 in the low half
@@ -1354,11 +1405,39 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
       S rr[NP], rz[NP];
 #pragma unroll
       for (int q = 0; q < NP; ++q) { rr[q] = S(0); rz[q] = S(0); }
-      if (any) {
+      // fused restriction: every piece of a segment with an active column
+      // sums its rows of each aggregate (the same decision in all of them)
+      bool rseg = false;
+      if constexpr (PC == kPrecTwoLevel) {
+        if (a.pc.agg_contig) {
+#pragma unroll
+          for (int q = 0; q < NP; ++q) rseg |= st_cur[s * NP + q] == kActive;
+        }
+      }
+      if (any || rseg) {
+        int cg = -1;  // aggregate being summed (warp-uniform)
+        S cacc[NP];
+#pragma unroll
+        for (int q = 0; q < NP; ++q) cacc[q] = S(0);
+        // the piece's first and last aggregates, and whether they go on
+        // beyond the piece (rows of other segments carry other labels)
+        int gF = -1, gL = -1;
+        bool hs = false, ts = false;
+        if constexpr (PC == kPrecTwoLevel) {
+          if (rseg) {
+            const int r0 = a.unit_row[u0], r1 = a.unit_row[u1];
+            gF = a.pc.agg[r0];
+            gL = a.pc.agg[r1 - 1];
+            hs = r0 > 0 && a.pc.agg[r0 - 1] == gF;
+            ts = r1 < a.n && a.pc.agg[r1] == gL;
+          }
+        }
         for (int u = u0; u < u1; ++u) {
           const int row = a.unit_row[u] + lane;
-          if (row < a.unit_row[u + 1]) {
-            V x[NP], pv[NP], qv[NP], r[NP];
+          const bool valid = row < a.unit_row[u + 1];
+          V r[NP];
+          if (valid) {
+            V x[NP], pv[NP], qv[NP];
             load_row<V, NP>(a.X, row, x);
             load_row<V, NP>(a.P, row, pv);
             load_row<V, NP>(a.Q, row, qv);
@@ -1375,7 +1454,35 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
             }
             store_row<V, NP>(a.X, row, x);
             store_row<V, NP>(a.R, row, r);
+          } else {
+#pragma unroll
+            for (int q = 0; q < NP; ++q) r[q] = V(0);
           }
+          if constexpr (PC == kPrecTwoLevel) {
+            if (rseg) {
+              // the unit's rows cover aggregates gl..gh, each a lane range
+              const int g = valid ? a.pc.agg[row] : -1;
+              const int gl = __shfl_sync(0xffffffffu, g, 0);
+              const int gh = __shfl_sync(0xffffffffu, g, a.unit_row[u + 1] - a.unit_row[u] - 1);
+              for (int gg = gl; gg >= 0 && gg <= gh; ++gg) {
+                if (gg != cg) {
+                  if (cg >= 0)
+                    restrict_flush<V, NP>(a, p, cg, hs && cg == gF, ts && cg == gL && !(hs && cg == gF), cacc);
+                  cg = gg;
+#pragma unroll
+                  for (int q = 0; q < NP; ++q) cacc[q] = S(0);
+                }
+                if (g == gg) {
+#pragma unroll
+                  for (int q = 0; q < NP; ++q) cacc[q] += (S)r[q];
+                }
+              }
+            }
+          }
+        }
+        if constexpr (PC == kPrecTwoLevel) {
+          if (rseg && cg >= 0)
+            restrict_flush<V, NP>(a, p, cg, hs && cg == gF, ts && cg == gL && !(hs && cg == gF), cacc);
         }
       }
       warp_store_partials<NP>(rr, part_rr + (int64_t)p * NP);
@@ -1390,9 +1497,12 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     mark(2);
 
     if constexpr (PC == kPrecTwoLevel) {
-      // ---- phases R, G: coarse correction of the new residual
-      coarse_restrict<V, NP>(a, st_cur, false);
-      if (!grid_sync(a.bar)) return;
+      // ---- phases R, G: coarse correction of the new residual (the
+      // restriction ran in phase B when aggregates are row ranges)
+      if (!a.pc.agg_contig) {
+        coarse_restrict<V, NP>(a, st_cur, false);
+        if (!grid_sync(a.bar)) return;
+      }
       mark(3);
       coarse_solve<V, NP>(a, st_cur, false, reinterpret_cast<float*>(stage_raw), kStageBytes / 4, c_bytes);
       if (!grid_sync(a.bar)) return;
@@ -1484,7 +1594,38 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
           }
         }
       }
-      if (any) {
+      if constexpr (PC == kPrecTwoLevel) {
+        if (!any) continue;
+        // z = dinv .* r + yc[agg]: the next unit's row range and aggregate
+        // labels are loaded one unit ahead, so the coarse value is not a
+        // second dependent round trip after the label
+        int rb = a.unit_row[u0], re = a.unit_row[u0 + 1];
+        int gn = rb + lane < re ? a.pc.agg[rb + lane] : -1;
+        for (int u = u0; u < u1; ++u) {
+          const int row = rb + lane;
+          const bool valid = row < re;
+          const int g = gn;
+          rb = re;
+          if (u + 1 < u1) {
+            re = a.unit_row[u + 2];
+            gn = rb + lane < re ? a.pc.agg[rb + lane] : -1;
+          }
+          if (valid) {
+            V r[NP], z[NP], pv[NP];
+            load_row<V, NP>(a.R, row, r);
+            load_row<V, NP>(a.P, row, pv);
+            const V d = a.pc.dinv[row];
+            V y[NP];
+            if (g >= 0) load_row<V, NP>(a.yc, g, y);
+#pragma unroll
+            for (int q = 0; q < NP; ++q) z[q] = d * r[q] + (g >= 0 ? y[q] : V(0));
+#pragma unroll
+            for (int q = 0; q < NP; ++q)
+              if (act[q]) pv[q] = z[q] + beta[q] * pv[q];
+            store_row<V, NP>(a.P, row, pv);
+          }
+        }
+      } else if (any) {  // Jacobi, IC(0), learned factor
         for (int u = u0; u < u1; ++u) {
           const int row = a.unit_row[u] + lane;
           if (row < a.unit_row[u + 1]) {
@@ -1642,6 +1783,7 @@ size_t pcg_workspace_bytes(int64_t n, int p, const ChunkTable& ct, int elem_size
   if (precond == kPrecTwoLevel) {
     b += 3 * a256(sizeof(double) * (size_t)std::max<int64_t>(nagg, 1) * p);
     b += a256(sizeof(double) * (size_t)(nagg + ct.nvc + 1) * p);  // coarse reduction slots
+    b += a256(sizeof(double) * 2 * (size_t)ct.npiece * p) + a256(sizeof(int32_t) * (size_t)std::max<int64_t>(nagg, 1));
   }
   return b + 256;
 }
@@ -1762,6 +1904,8 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
       return LAPY_ERR_WORKSPACE;
     }
     a.aslot = (S*)w; w += a256(sizeof(double) * (size_t)(pc.nagg + ct.nvc + 1) * p);
+    a.rc_part = (S*)w; w += a256(sizeof(double) * 2 * (size_t)ct.npiece * p);
+    a.rc_cnt = (int32_t*)w; w += a256(sizeof(int32_t) * (size_t)std::max(pc.nagg, 1));
   }
   a.state_out = state_dev;
   a.rtol2 = (S)(rtol * rtol);
@@ -1776,8 +1920,10 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   // every slot is rewritten by each fold; cleared once so that none is ever
   // read uninitialised
   LAPY_CUDA_TRY(cudaMemsetAsync(a.slot, 0, sizeof(double) * 3 * (size_t)ct.nslot * p, stream));
-  if (pc.kind == kPrecTwoLevel)
+  if (pc.kind == kPrecTwoLevel) {
     LAPY_CUDA_TRY(cudaMemsetAsync(a.aslot, 0, sizeof(double) * (size_t)std::max(pc.naslot, 1) * p, stream));
+    LAPY_CUDA_TRY(cudaMemsetAsync(a.rc_cnt, 0, sizeof(int32_t) * (size_t)std::max(pc.nagg, 1), stream));
+  }
   LAPY_CUDA_TRY(cudaMemsetAsync(a.slot64, 0, sizeof(double) * (size_t)ct.nslot * p, stream));
   if (ru) LAPY_CUDA_TRY(cudaMemsetAsync(a.ru_col, 0, sizeof(int32_t) * 2 * (size_t)ct.nseg * p, stream));
   // segments without rows have no piece: they are reported as solved
@@ -1837,7 +1983,7 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
     unsigned long long cbytes;
     memcpy(&cbytes, &hctl[28], 8);
     lapy_profile_add_pcg(ms, (long long)hctl[2], (long long)rows, (long long)nnz, p, (int)sizeof(V), pc.kind,
-                         (double)cbytes);
+                         (double)cbytes, pc.kind == kPrecTwoLevel && pc.agg_contig != 0);
     double phase_ms[kPcgPhases];
     for (int k = 0; k < kPcgPhases; ++k) {
       unsigned long long ns;
