@@ -369,6 +369,8 @@ def run_gpu(args, rank, world):
         "lanczos": {"segment_steps": prof["lanczos_segment_steps"], "second_cgs_passes": prof["second_cgs_passes"]},
         "wall_s": wall,
     }
+    if not args.no_spmm:
+        line["spmm"] = run_spmm(batch_in, hbm, peak_kind)
     heat_x = None
     if not args.no_heat:
         line["heat"], heat_x = run_heat(args, meshes, lv, batch_in, world)
@@ -400,6 +402,42 @@ def _timed(fn, steps, warmup):
     ev1.record()
     torch.cuda.synchronize()
     return ev0.elapsed_time(ev1) / 1e3
+
+
+def run_spmm(batch_in, hbm, peak_kind, reps=20, warmup=3):
+    """The pipelined FP32 SELL product alone on the headline batch's stiffness
+    matrix (the PCG's SpMM outside the persistent kernel), p = 1 and 4
+    columns: algorithmic bytes (value + column index per nonzero, X read once,
+    Y written) over the CUDA-event time of one product."""
+    import torch
+
+    from lapy_gb300 import _device, shapedna
+
+    fem = shapedna.BatchedFEM.from_input(batch_in, lump=False)
+    sell = _device.SellF32(fem.indptr, fem.indices, fem.a_vals, fem.n, fem.nnz, seg_row=batch_in.seg_row)
+    out = {"kernel": "sell_spmm_pipe_kernel (FP32 SELL, cp.async slice pipeline)", "rows": fem.n, "nnz": fem.nnz,
+           "peak": hbm, "peak_kind": f"{peak_kind} hbm_gbs",
+           "l2": "matrix (8 B per nonzero) >> 129 MB L2; X may stay in L2"}
+    g = torch.Generator(device="cuda").manual_seed(7)
+    for p in (1, 4):
+        x = torch.randn(fem.n, p, device="cuda", dtype=torch.float32, generator=g)
+        y = torch.empty_like(x)
+        for _ in range(warmup):
+            sell.spmm(x, y)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            sell.spmm(x, y)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        nbytes = fem.nnz * 8 + 2 * fem.n * p * 4
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out[f"p{p}"] = {"ms": ms, "bytes": nbytes, "achieved_gbs": gbs, "frac": gbs / hbm}
+    del sell, fem
+    return out
 
 
 def run_heat(args, meshes, lv, batch_in, world):
@@ -457,8 +495,10 @@ def run_learned(args):
 
     net, hist = spai_train.train(n_meshes=128, level=6, systems=4096, batch=32, seed=args.seed)
     ev = spai_train.evaluate(net, n_test=args.learned_test, level=7, seed=args.seed + 1)
-    return {"train": hist, "test": ev,
-            "note": "factored SPAI G'G (per-edge MLP, BF16 weights) vs Jacobi; same PCG, same tolerance"}
+    ev4 = spai_train.evaluate(net, n_test=args.learned_test, level=7, seed=args.seed + 1, cols=4)
+    return {"train": hist, "test": ev, "test_block4": ev4,
+            "note": "factored SPAI G'G (per-edge MLP, BF16 weights) vs Jacobi and IC(0); same PCG, same tolerance; "
+                    "test: one right-hand side per mesh, test_block4: four solved together (a Lanczos block)"}
 
 
 def run_plain_spectra(args, meshes, lv, batched_per_gpu):
@@ -738,6 +778,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-timeout", type=float, default=600.0, help="single-mesh workloads: CPU run time limit (s)")
     ap.add_argument("--no-heat", action="store_true")
+    ap.add_argument("--no-spmm", action="store_true", help="skip the standalone SELL SpMM leg")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-test", type=int, default=32, help="held-out level-7 meshes of the learned-SPAI leg")

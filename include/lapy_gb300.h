@@ -189,6 +189,25 @@ int lapy_csr_spmm_f64(int64_t n, const int32_t* indptr, const int32_t* indices,
 int lapy_csr_spmm_f32(int64_t n, const int32_t* indptr, const int32_t* indices,
                       const float* vals, int ncol, const float* x, float* y,
                       float alpha, float beta, int group, void* stream);
+/* Standalone FP32 SELL product Y = Mat X (X, Y row-major n x ncol, ncol in
+ * {1, 2, 4, 8}): the sliced-ELL copy (32-row slices) and the pipelined
+ * product of the inner PCG, outside the persistent kernel.  It stands for
+ * the sparse products inside the reference's ARPACK/SuperLU operator
+ * (solver.py:707-713) when measured alone.  _build casts vals to FP32 and
+ * builds the slices into `work` (size from _workspace_bytes); the handle
+ * points into `work`, which must outlive it. */
+typedef struct {
+  int32_t nunit;             /* 32-row units */
+  const int32_t* unit_row;   /* device, nunit + 1 */
+  const int32_t* slice_ptr;  /* device, nunit + 1 */
+  const int32_t* col;        /* device */
+  const float* val;          /* device */
+} lapy_sell_f32;
+size_t lapy_sell_f32_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row);
+int lapy_sell_f32_build(int64_t n, const int32_t* indptr, const int32_t* indices, const double* vals,
+                        int64_t nnz, int nseg, const int32_t* seg_row, lapy_sell_f32* out, void* work,
+                        size_t ws_bytes, void* stream);
+int lapy_sell_f32_spmm(const lapy_sell_f32* m, int ncol, const float* x, float* y, void* stream);
 /* Diagonal-matrix variant Y = alpha * diag(d) X + beta * Y. */
 int lapy_diag_mm_f64(int64_t n, const double* d, int ncol, const double* x, double* y,
                      double alpha, double beta, void* stream);

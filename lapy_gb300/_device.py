@@ -290,6 +290,30 @@ def pcg_solve(indptr, indices, k_vals, n, nnz, b: torch.Tensor, rtol: float, max
     return (X[:, 0] if squeeze else X), relres, int(iters.value)
 
 
+class SellF32:
+    """FP32 SELL copy of a CSR matrix (float64 values cast) for the standalone
+    pipelined product ``Y = Mat X`` (X, Y: n x ncol float32, ncol in 1, 2, 4, 8)."""
+
+    def __init__(self, indptr, indices, vals, n: int, nnz: int, seg_row=None):
+        L = _lib.lib()
+        seg = np.ascontiguousarray(seg_row if seg_row is not None else [0, n], dtype=np.int32)
+        self.n = n
+        self.nnz = nnz
+        self.ws = workspace(L.lapy_sell_f32_workspace_bytes(n, nnz, len(seg) - 1, seg.ctypes.data))
+        self.handle = _lib.SellF32()
+        _lib.check(L.lapy_sell_f32_build(n, dptr(indptr), dptr(indices), dptr(vals), nnz, len(seg) - 1,
+                                         seg.ctypes.data, C.byref(self.handle), dptr(self.ws), self.ws.numel(),
+                                         stream()), "sell_f32_build")
+
+    def spmm(self, x: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
+        ncol = 1 if x.dim() == 1 else x.shape[1]
+        if x.dtype != torch.float32 or y.dtype != torch.float32 or not x.is_contiguous() or not y.is_contiguous():
+            raise ValueError("SellF32.spmm wants contiguous float32 x and y")
+        _lib.check(_lib.lib().lapy_sell_f32_spmm(C.byref(self.handle), ncol, dptr(x), dptr(y), stream()),
+                   "sell_f32_spmm")
+        return y
+
+
 def ic0_pcg_solve(indptr, indices, k_vals, n, nnz, b: torch.Tensor, rtol: float, maxiter: int = 20000,
                   inner_rtol: float = 1e-4, seg_row=None):
     """Solve K X = B with IC(0)-preconditioned PCG (FP32 iterations inside FP64

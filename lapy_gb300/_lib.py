@@ -46,6 +46,13 @@ class EigsTuning(C.Structure):
                 ("fold_aggs", C.c_int), ("ctas_per_sm", C.c_int)]
 
 
+class SellF32(C.Structure):
+    """``lapy_sell_f32`` (include/lapy_gb300.h): a SELL copy in a workspace."""
+
+    _fields_ = [("nunit", C.c_int32), ("unit_row", C.c_void_p), ("slice_ptr", C.c_void_p), ("col", C.c_void_p),
+                ("val", C.c_void_p)]
+
+
 _i32p = C.c_void_p
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -86,6 +93,9 @@ _SIGNATURES = {
     "lapy_csr_seg_axpby": (_int, [_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _vp, _vp]),
     "lapy_csr_spmm_f64": (_int, [_i64, _vp, _vp, _vp, _int, _vp, _vp, _dbl, _dbl, _int, _vp]),
     "lapy_csr_spmm_f32": (_int, [_i64, _vp, _vp, _vp, _int, _vp, _vp, C.c_float, C.c_float, _int, _vp]),
+    "lapy_sell_f32_workspace_bytes": (C.c_size_t, [_i64, _i64, _int, _vp]),
+    "lapy_sell_f32_build": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, C.POINTER(SellF32), _vp, C.c_size_t, _vp]),
+    "lapy_sell_f32_spmm": (_int, [C.POINTER(SellF32), _int, _vp, _vp, _vp]),
     "lapy_diag_mm_f64": (_int, [_i64, _vp, _int, _vp, _vp, _dbl, _dbl, _vp]),
     "lapy_vec_axpby": (_int, [_i64, _dbl, _vp, _dbl, _vp, _vp, _vp]),
     "lapy_heat_product_f64": (_int, [_i64, _vp, _vp, _i64, _int, _int, _vp, _int, _vp, _vp]),

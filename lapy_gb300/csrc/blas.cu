@@ -17,14 +17,92 @@ __global__ void seg_col_norm2_kernel(const double* __restrict__ x, const double*
   }
 }
 
-int seg_col_norm2(const double* x, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream) {
-  seg_col_norm2_kernel<<<ct.nseg, 256, 0, stream>>>(x, x, ncol, ct.seg_row, out);
+// Per-chunk column sums of x .* y (NC columns, one CTA per chunk, every
+// thread accumulating all columns of its rows), then per segment the sum of
+// its chunks' partials in chunk order: reproducible, and a large segment is
+// spread over many CTAs instead of one.
+template <int NC>
+__global__ void __launch_bounds__(256) chunk_col_dot_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                                                            const int32_t* __restrict__ chunk_row,
+                                                            double* __restrict__ part) {
+  __shared__ double sh[NC][8];
+  const int c = blockIdx.x;
+  const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
+  double acc[NC];
+#pragma unroll
+  for (int q = 0; q < NC; ++q) acc[q] = 0.0;
+#pragma unroll 2
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const double* xr = x + r * NC;
+    const double* yr = y + r * NC;
+    if constexpr (NC % 2 == 0) {
+#pragma unroll
+      for (int q = 0; q < NC; q += 2) {
+        const double2 a = *reinterpret_cast<const double2*>(xr + q);
+        const double2 b = *reinterpret_cast<const double2*>(yr + q);
+        acc[q] += a.x * b.x;
+        acc[q + 1] += a.y * b.y;
+      }
+    } else {
+      acc[0] += xr[0] * yr[0];
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    const double v = warp_sum(acc[q]);
+    if (lane == 0) sh[q][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += sh[threadIdx.x][w];
+    part[(int64_t)c * kChunkScratch + threadIdx.x] = t;
+  }
+}
+
+__global__ void seg_sum_chunks_kernel(int nseg, int ncol, const int32_t* __restrict__ seg_chunk,
+                                      const double* __restrict__ part, double* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nseg * ncol) return;
+  const int s = t / ncol, q = t - s * ncol;
+  double acc = 0.0;
+  for (int k = seg_chunk[s]; k < seg_chunk[s + 1]; ++k) acc += part[(int64_t)k * kChunkScratch + q];
+  out[t] = acc;
+}
+
+template <int NC>
+static int chunked_dot(const double* x, const double* y, const ChunkTable& ct, double* out, cudaStream_t stream) {
+  chunk_col_dot_kernel<NC><<<ct.nchunk, 256, 0, stream>>>(x, y, ct.chunk_row, ct.scratch);
+  LAPY_TRY(lapy_check_launch("chunk_col_dot_kernel"));
+  seg_sum_chunks_kernel<<<lapy_ceil_div(ct.nseg * NC, 128), 128, 0, stream>>>(ct.nseg, NC, ct.seg_chunk, ct.scratch,
+                                                                              out);
+  return lapy_check_launch("seg_sum_chunks_kernel");
+}
+
+static int seg_dot_any(const double* x, const double* y, int ncol, const ChunkTable& ct, double* out,
+                       cudaStream_t stream) {
+  if (ct.scratch && ct.nchunk > 0) {
+    switch (ncol) {
+      case 1: return chunked_dot<1>(x, y, ct, out, stream);
+      case 2: return chunked_dot<2>(x, y, ct, out, stream);
+      case 4: return chunked_dot<4>(x, y, ct, out, stream);
+      case 8: return chunked_dot<8>(x, y, ct, out, stream);
+      case 16: return chunked_dot<16>(x, y, ct, out, stream);
+      default: break;
+    }
+  }
+  seg_col_norm2_kernel<<<ct.nseg, 256, 0, stream>>>(x, y, ncol, ct.seg_row, out);
   return lapy_check_launch("seg_col_norm2_kernel");
 }
 
+int seg_col_norm2(const double* x, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream) {
+  return seg_dot_any(x, x, ncol, ct, out, stream);
+}
+
 int seg_col_dot(const double* x, const double* y, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream) {
-  seg_col_norm2_kernel<<<ct.nseg, 256, 0, stream>>>(x, y, ncol, ct.seg_row, out);
-  return lapy_check_launch("seg_col_norm2_kernel");
+  return seg_dot_any(x, y, ncol, ct, out, stream);
 }
 
 __global__ void cast_kernel(int64_t n, const double* __restrict__ x, float* __restrict__ y) {

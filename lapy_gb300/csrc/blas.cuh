@@ -5,7 +5,8 @@
 
 namespace lapy {
 
-// out[s*ncol + c] = sum over rows of segment s of x[row*ncol + c]^2 (one CTA per segment)
+// out[s*ncol + c] = sum over rows of segment s of x[row*ncol + c]^2 (per-chunk partials in the
+// chunk table's scratch, then per segment in chunk order)
 int seg_col_norm2(const double* x, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream);
 // out[s*ncol + c] = sum over segment s's rows of x(row, c) * y(row, c)
 int seg_col_dot(const double* x, const double* y, int ncol, const ChunkTable& ct, double* out, cudaStream_t stream);

@@ -398,6 +398,100 @@ __global__ void __launch_bounds__(256) gemm_tn_dfany_kernel(const float2* __rest
   partial[((int64_t)c * na + a) * nb + b] = (double)sh + (double)sl;
 }
 
+// Register-tiled forms of the two products above.
+//
+// NN: Y(row, b0 + t) = sum_a X(row, a) H_s[a][b0 + t], t < TB, for a
+// double-float X stored as blocks of bs columns (block stride bst float2;
+// bs = na for a row-major matrix) and a double-float H whose TB columns the
+// CTA stages in shared memory (na x TB).  One thread per row holds TB
+// accumulators, so every X value is read once per column tile instead of once
+// per output.
+constexpr int kNnTile = 16;
+template <int TB>
+__global__ void __launch_bounds__(256) gemm_nn_df_tile_kernel(const float2* __restrict__ X, int bs, int64_t bst,
+                                                              int na, const float2* __restrict__ H,
+                                                              int64_t h_seg_stride, int ldh, double* __restrict__ Y,
+                                                              int ldy, int nb, const int32_t* __restrict__ chunk_row,
+                                                              const int32_t* __restrict__ chunk_seg) {
+  extern __shared__ float2 hs[];  // na x TB
+  const int c = blockIdx.x, b0 = blockIdx.y * TB;
+  const float2* Hs = H + (int64_t)chunk_seg[c] * h_seg_stride;
+  for (int i = threadIdx.x; i < na * TB; i += blockDim.x) {
+    const int a = i / TB, b = b0 + i % TB;
+    hs[i] = b < nb ? Hs[(int64_t)a * ldh + b] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int64_t r1 = chunk_row[c + 1];
+  for (int64_t row = chunk_row[c] + threadIdx.x; row < r1; row += blockDim.x) {
+    float sh[TB], sl[TB];
+#pragma unroll
+    for (int t = 0; t < TB; ++t) { sh[t] = 0.f; sl[t] = 0.f; }
+    for (int a0 = 0; a0 < na; a0 += bs) {
+      const float2* xr = X + (int64_t)(a0 / bs) * bst + row * bs;
+      const int w = min(bs, na - a0);
+      for (int q = 0; q < w; ++q) {
+        const float2 x = xr[q];
+        const float2* h = hs + (a0 + q) * TB;
+#pragma unroll
+        for (int t = 0; t < TB; ++t) df_fma(x, h[t], sh[t], sl[t]);
+      }
+    }
+    double* yr = Y + row * ldy + b0;
+#pragma unroll
+    for (int t = 0; t < TB; ++t)
+      if (b0 + t < nb) yr[t] = (double)sh[t] + (double)sl[t];
+  }
+}
+
+// TN: partial[c][a][b] = sum over chunk c's rows of X(row, a) Y(row, b) for
+// row-major double-float X (n x na) and Y (n x nb).  A CTA computes a 64 x 64
+// output tile (grid.y, grid.z), each thread 4 x 4 of it; rows pass through
+// shared memory 16 at a time.
+constexpr int kTnRows = 16;
+__global__ void __launch_bounds__(256) gemm_tn_df_tile_kernel(const float2* __restrict__ X, int na,
+                                                              const float2* __restrict__ Y, int nb,
+                                                              const int32_t* __restrict__ chunk_row,
+                                                              double* __restrict__ partial) {
+  __shared__ float2 sx[kTnRows][64];
+  __shared__ float2 sy[kTnRows][64];
+  const int c = blockIdx.x, a0 = blockIdx.y * 64, b0 = blockIdx.z * 64;
+  const int ta = (threadIdx.x >> 4) * 4, tb = (threadIdx.x & 15) * 4;
+  float sh[4][4], sl[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { sh[i][j] = 0.f; sl[i][j] = 0.f; }
+  const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
+  for (int64_t rt = r0; rt < r1; rt += kTnRows) {
+    __syncthreads();  // the previous tile is consumed
+    for (int i = threadIdx.x; i < kTnRows * 64; i += blockDim.x) {
+      const int r = i >> 6, col = i & 63;
+      const int64_t row = rt + r;
+      const bool ok = row < r1;
+      sx[r][col] = (ok && a0 + col < na) ? X[row * na + a0 + col] : make_float2(0.f, 0.f);
+      sy[r][col] = (ok && b0 + col < nb) ? Y[row * nb + b0 + col] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int r = 0; r < kTnRows; ++r) {
+      float2 xa[4], yb[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { xa[i] = sx[r][ta + i]; yb[i] = sy[r][tb + i]; }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) df_fma(xa[i], yb[j], sh[i][j], sl[i][j]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int a = a0 + ta + i, b = b0 + tb + j;
+      if (a < na && b < nb) partial[((int64_t)c * na + a) * nb + b] = (double)sh[i][j] + (double)sl[i][j];
+    }
+}
+
 // Selective second CGS pass: segment s repeats the projection when the first
 // pass cancelled more than a factor 1/eta of some column's M-norm
 // (||W'||^2 < eta^2 ||W||^2, NaN included); otherwise one FP64 pass already
@@ -448,24 +542,50 @@ __global__ void chol_small_kernel(int nseg, int p, const double* __restrict__ G,
   fail[s] = bad;
 }
 
-// W(row, :) = W(row, :) * R_s^-1  (R upper triangular, p x p)
-__global__ void trsm_right_kernel(double* __restrict__ W, int p, const double* __restrict__ R,
-                                  const int32_t* __restrict__ chunk_row, const int32_t* __restrict__ chunk_seg,
-                                  int nchunk) {
+// W(row, :) = W(row, :) * R_s^-1  (R upper triangular, p x p): R and the
+// reciprocals of its diagonal staged in shared memory once per chunk, so a
+// row costs p(p+1)/2 FMAs and no division (FP64 division is slow here).
+template <int PT>
+__global__ void trsm_right_kernel(double* __restrict__ W, const double* __restrict__ R,
+                                  const int32_t* __restrict__ chunk_row, const int32_t* __restrict__ chunk_seg) {
+  __shared__ double sr[PT * PT];
+  __shared__ double sinv[PT];
   const int c = blockIdx.x;
   const int s = chunk_seg[c];
-  const double* r = R + (int64_t)s * p * p;
+  const double* r = R + (int64_t)s * PT * PT;
+  for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) sr[e] = r[e];
+  if (threadIdx.x < PT) sinv[threadIdx.x] = 1.0 / r[threadIdx.x * PT + threadIdx.x];
+  __syncthreads();
   const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
   for (int64_t row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
-    double x[16];
-    double* w = W + row * p;
-    for (int j = 0; j < p; ++j) {
-      double v = w[j];
-      for (int i = 0; i < j; ++i) v -= x[i] * r[i * p + j];
-      x[j] = v / r[j * p + j];
+    double x[PT];
+    double* w = W + row * PT;
+#pragma unroll
+    for (int j = 0; j < PT; ++j) x[j] = w[j];
+#pragma unroll
+    for (int j = 0; j < PT; ++j) {
+      double v = x[j];
+#pragma unroll
+      for (int i = 0; i < j; ++i) v -= x[i] * sr[i * PT + j];
+      x[j] = v * sinv[j];
     }
-    for (int j = 0; j < p; ++j) w[j] = x[j];
+#pragma unroll
+    for (int j = 0; j < PT; ++j) w[j] = x[j];
   }
+}
+
+static int launch_trsm_right(double* W, int p, const double* R, const ChunkTable& gt, cudaStream_t st) {
+  switch (p) {
+    case 1: trsm_right_kernel<1><<<gt.nchunk, 128, 0, st>>>(W, R, gt.chunk_row, gt.chunk_seg); break;
+    case 2: trsm_right_kernel<2><<<gt.nchunk, 128, 0, st>>>(W, R, gt.chunk_row, gt.chunk_seg); break;
+    case 4: trsm_right_kernel<4><<<gt.nchunk, 128, 0, st>>>(W, R, gt.chunk_row, gt.chunk_seg); break;
+    case 8: trsm_right_kernel<8><<<gt.nchunk, 128, 0, st>>>(W, R, gt.chunk_row, gt.chunk_seg); break;
+    case 16: trsm_right_kernel<16><<<gt.nchunk, 128, 0, st>>>(W, R, gt.chunk_row, gt.chunk_seg); break;
+    default:
+      lapy_set_last_message("eigs: block width %d not in {1,2,4,8,16}", p);
+      return LAPY_ERR_INVALID;
+  }
+  return lapy_check_launch("trsm_right_kernel");
 }
 
 // C_s = A_s * B_s for p x p (used for B_j = R2 R1)
@@ -946,8 +1066,7 @@ struct EigOps {
       double* R = pass == 0 ? e.R1 : e.R2;
       chol_small_kernel<<<lapy_ceil_div(P.nseg, 64), 64, 0, st>>>(P.nseg, p, e.G, R, e.active, e.fail);
       LAPY_TRY(lapy_check_launch("chol_small_kernel"));
-      trsm_right_kernel<<<P.gt.nchunk, 128, 0, st>>>(W, p, R, P.gt.chunk_row, P.gt.chunk_seg, P.gt.nchunk);
-      LAPY_TRY(lapy_check_launch("trsm_right_kernel"));
+      LAPY_TRY(launch_trsm_right(W, p, R, P.gt, st));
     }
     small_matmul_kernel<<<P.nseg, 64, 0, st>>>(P.nseg, p, e.R2, e.R1, e.Bm);
     return lapy_check_launch("small_matmul_kernel");
@@ -1206,10 +1325,26 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     to_df_kernel<<<lapy_ceil_div(m, 256), 256, 0, st>>>(m, x, y);
     return lapy_check_launch("to_df_kernel");
   };
+  // Y = X H per segment in double-float, register-tiled (H's columns staged in
+  // shared memory); the one-thread-per-entry form when H is too tall for it
+  auto gemm_nn_df_tiled = [&](const float2* X, int bs, int64_t bst, int na, const float2* H, int64_t hstride,
+                              int ldh, double* Y, int ldy, int nb) -> int {
+    constexpr size_t kSmemMax = 96 * 1024;
+    const size_t smem = sizeof(float2) * (size_t)na * kNnTile;
+    if (smem > kSmemMax) {
+      gemm_nn_dfany_kernel<<<P.gt.nchunk, 256, 0, st>>>(X, bs, bst, na, H, hstride, ldh, Y, ldy, nb, P.gt.chunk_row,
+                                                        P.gt.chunk_seg);
+      return lapy_check_launch("gemm_nn_dfany_kernel");
+    }
+    LAPY_CUDA_TRY(cudaFuncSetAttribute(gemm_nn_df_tile_kernel<kNnTile>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kSmemMax));
+    dim3 grid(P.gt.nchunk, lapy_ceil_div(nb, kNnTile));
+    gemm_nn_df_tile_kernel<kNnTile><<<grid, 256, smem, st>>>(X, bs, bst, na, H, hstride, ldh, Y, ldy, nb,
+                                                             P.gt.chunk_row, P.gt.chunk_seg);
+    return lapy_check_launch("gemm_nn_df_tile_kernel");
+  };
   LAPY_TRY(to_df(e.Sfinal, e.S_df, (int64_t)ns * lda * keff));
-  gemm_nn_dfany_kernel<<<P.gt.nchunk, 256, 0, st>>>(e.basis_df, p, n * p, nb_used, e.S_df, (int64_t)lda * keff,
-                                                    keff, e.X, keff, keff, P.gt.chunk_row, P.gt.chunk_seg);
-  LAPY_TRY(lapy_check_launch("gemm_nn_dfany_kernel"));
+  LAPY_TRY(gemm_nn_df_tiled(e.basis_df, p, n * p, nb_used, e.S_df, (int64_t)lda * keff, keff, e.X, keff, keff));
   // final Rayleigh-Ritz with the exact A and M (projections in double-float;
   // AX and MX are only read by them, so they are split in place)
   LAPY_TRY(csr_spmm<double>(n, indptr, indices, a_vals, keff, e.X, e.AX, 1.0, 0.0, G, st));
@@ -1220,17 +1355,17 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     LAPY_TRY(lapy_check_launch("to_df_inplace_kernel"));
   }
   {
-    dim3 grid(P.gt.nchunk, lapy_ceil_div(keff, kTile), lapy_ceil_div(keff, kTile));
+    dim3 grid(P.gt.nchunk, lapy_ceil_div(keff, 64), lapy_ceil_div(keff, 64));
     dim3 g2(P.nseg, std::max(1u, std::min(64u, lapy_ceil_div((int64_t)keff * keff, 256))));
-    gemm_tn_dfany_kernel<<<grid, 256, 0, st>>>(e.X_df, keff, reinterpret_cast<const float2*>(e.AX), keff,
-                                               P.gt.chunk_row, e.partial);
-    LAPY_TRY(lapy_check_launch("gemm_tn_dfany_kernel"));
+    gemm_tn_df_tile_kernel<<<grid, 256, 0, st>>>(e.X_df, keff, reinterpret_cast<const float2*>(e.AX), keff,
+                                                 P.gt.chunk_row, e.partial);
+    LAPY_TRY(lapy_check_launch("gemm_tn_df_tile_kernel"));
     gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, keff, keff, P.gt.seg_chunk, e.Ak, (int64_t)keff * keff,
                                               keff);
     LAPY_TRY(lapy_check_launch("gemm_tn_reduce_kernel"));
-    gemm_tn_dfany_kernel<<<grid, 256, 0, st>>>(e.X_df, keff, reinterpret_cast<const float2*>(e.MX), keff,
-                                               P.gt.chunk_row, e.partial);
-    LAPY_TRY(lapy_check_launch("gemm_tn_dfany_kernel"));
+    gemm_tn_df_tile_kernel<<<grid, 256, 0, st>>>(e.X_df, keff, reinterpret_cast<const float2*>(e.MX), keff,
+                                                 P.gt.chunk_row, e.partial);
+    LAPY_TRY(lapy_check_launch("gemm_tn_df_tile_kernel"));
     gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, keff, keff, P.gt.seg_chunk, e.Mk, (int64_t)keff * keff,
                                               keff);
     LAPY_TRY(lapy_check_launch("gemm_tn_reduce_kernel"));
@@ -1242,13 +1377,15 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
   LAPY_TRY(sym_eig_top(ns, e.Cneg, keff, e.nsize, k, e.theta2, e.V, e.eigw2, nullptr, st));
   rr_finish_kernel<<<ns, 128, 0, st>>>(keff, k, e.Mk, e.V, e.theta2, evals);
   LAPY_TRY(lapy_check_launch("rr_finish_kernel"));
-  BMat X2{e.X, keff, 0};
+  // eigenvectors X V in double-float (X_df holds X; V split into S_df, which
+  // is free now)
+  LAPY_TRY(to_df(e.V, e.S_df, (int64_t)ns * keff * k));
   if (reorder) {  // eigenvectors in the system's order, then back to the caller's (AX is free here)
-    LAPY_TRY(ops.gemm_nn(X2, keff, e.V, (int64_t)keff * k, k, e.AX, k, k, 1.0, 0.0, nullptr));
+    LAPY_TRY(gemm_nn_df_tiled(e.X_df, keff, 0, keff, e.S_df, (int64_t)keff * k, k, e.AX, k, k));
     unpermute_rows_kernel<<<lapy_ceil_div(n * k, 256), 256, 0, st>>>(n, k, e.perm, e.AX, evecs);
     LAPY_TRY(lapy_check_launch("unpermute_rows_kernel"));
   } else {
-    LAPY_TRY(ops.gemm_nn(X2, keff, e.V, (int64_t)keff * k, k, evecs, k, k, 1.0, 0.0, nullptr));
+    LAPY_TRY(gemm_nn_df_tiled(e.X_df, keff, 0, keff, e.S_df, (int64_t)keff * k, k, evecs, k, k));
   }
   LAPY_CUDA_TRY(cudaMemcpyAsync(hfail.data(), e.fail, 4 * ns, cudaMemcpyDeviceToHost, st));
   LAPY_CUDA_TRY(cudaStreamSynchronize(st));

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstring>
 #include "pcg.cuh"
+#include "blas.cuh"
 #include "scan.cuh"
 
 namespace lapy {
@@ -130,7 +131,7 @@ size_t chunk_table_bytes(const ChunkTable& ct) {
   return a256(4 * (size_t)(ct.nchunk + 1)) + a256(4 * (size_t)ct.nchunk) + a256(4 * (size_t)(ct.nseg + 1)) * 3 +
          a256(4 * (size_t)(ct.nunit + 1)) + a256(4 * (size_t)(ct.npiece + 1)) + a256(4 * (size_t)ct.npiece) +
          a256(4 * (size_t)(ct.nvw + 1)) + a256(4 * (size_t)(ct.nvc + 1)) + a256(4 * (size_t)(ct.nseg + 1)) +
-         a256(4 * (size_t)std::max(ct.nseg, 1));
+         a256(4 * (size_t)std::max(ct.nseg, 1)) + a256(8 * (size_t)kChunkScratch * std::max(ct.nchunk, 1));
 }
 
 int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream) {
@@ -153,6 +154,8 @@ int upload_chunk_table(ChunkTable* ct, void* mem, cudaStream_t stream) {
   LAPY_TRY(put(&ct->vc_piece, ct->h_vc_piece));
   LAPY_TRY(put(&ct->seg_slot, ct->h_seg_slot));
   LAPY_TRY(put(&ct->seg_vc0, ct->h_seg_vc0));
+  ct->scratch = (double*)p;
+  p += a256(8 * (size_t)kChunkScratch * std::max(ct->nchunk, 1));
   // pageable sources: the copies must complete before the host vectors change
   LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
   return LAPY_OK;
@@ -2030,7 +2033,113 @@ template int pcg_solve<double>(int64_t, const int32_t*, const int32_t*, const do
                                double*, double, int, int32_t*, void*, size_t, cudaStream_t, int*,
                                const PcgTuning*);
 
+// Standalone FP32 SELL product Y = Mat X (row-major n x NP): the PCG's SpMM
+// outside the persistent kernel.  Every warp takes a contiguous range of
+// units and runs them through the same cp.async double-buffered slice
+// pipeline as the PCG (sell_piece_spmm).
+template <int NP>
+__global__ void __launch_bounds__(256) sell_spmm_pipe_kernel(SellMatrix<float> M, const int32_t* __restrict__ unit_row,
+                                                             int nunit, const float* __restrict__ X,
+                                                             float* __restrict__ Y) {
+  __shared__ __align__(16) float slots[kWarps][2 * kSellShort * 32 * 2];
+  const int warp = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * kWarps + warp, nw = (int64_t)gridDim.x * kWarps;
+  const int u0 = (int)(nunit * gw / nw), u1 = (int)(nunit * (gw + 1) / nw);
+  if (u0 >= u1) return;
+  float dummy[NP];
+  sell_piece_spmm<NP, false>(M, X, Y, nullptr, unit_row, u0, u1, slots[warp], dummy);
+}
+
+template <int NP>
+static int launch_sell_pipe(const SellMatrix<float>& M, const int32_t* unit_row, int nunit, const float* X, float* Y,
+                            cudaStream_t stream) {
+  int per_sm = 0;
+  LAPY_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sell_spmm_pipe_kernel<NP>, 256, 0));
+  per_sm = std::max(1, per_sm);
+  const int grid = std::max(1, std::min(per_sm * lapy_num_sms(), (nunit + kWarps - 1) / kWarps));
+  sell_spmm_pipe_kernel<NP><<<grid, 256, 0, stream>>>(M, unit_row, nunit, X, Y);
+  return lapy_check_launch("sell_spmm_pipe_kernel");
+}
+
 }  // namespace lapy
+
+// Standalone SELL product: workspace = chunk table, FP32 values, SELL copy.
+static size_t sell_f32_layout(int64_t nnz, const lapy::ChunkTable& ct, size_t* off_vals, size_t* off_sell) {
+  using namespace lapy;
+  size_t off = a256(chunk_table_bytes(ct));
+  *off_vals = off;
+  off += a256(4 * (size_t)nnz);
+  *off_sell = off;
+  return off + sell_bytes_bound(nnz, ct, sizeof(float)) + 256;
+}
+
+extern "C" size_t lapy_sell_f32_workspace_bytes(int64_t n, int64_t nnz, int nseg, const int32_t* seg_row) {
+  using namespace lapy;
+  if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row) return 0;
+  ChunkTable ct;
+  plan_chunks(seg_row, nseg, 4 * lapy_num_sms(), &ct);
+  size_t a, b;
+  return sell_f32_layout(nnz, ct, &a, &b);
+}
+
+extern "C" int lapy_sell_f32_build(int64_t n, const int32_t* indptr, const int32_t* indices, const double* vals,
+                                   int64_t nnz, int nseg, const int32_t* seg_row, lapy_sell_f32* out, void* work,
+                                   size_t ws_bytes, void* stream_) {
+  using namespace lapy;
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n <= 0 || nnz <= 0 || nseg <= 0 || !seg_row || !indptr || !indices || !vals || !out || !work) {
+    lapy_set_last_message("sell_f32_build: invalid arguments");
+    return LAPY_ERR_INVALID;
+  }
+  if (seg_row[0] != 0 || seg_row[nseg] != n) {
+    lapy_set_last_message("sell_f32_build: segment rows must span [0, n)");
+    return LAPY_ERR_INVALID;
+  }
+  ChunkTable ct;
+  plan_chunks(seg_row, nseg, 4 * lapy_num_sms(), &ct);
+  size_t off_vals, off_sell;
+  const size_t need = sell_f32_layout(nnz, ct, &off_vals, &off_sell);
+  if (ws_bytes < need) return LAPY_ERR_WORKSPACE;
+  char* base = (char*)(((uintptr_t)work + 255) & ~uintptr_t(255));
+  LAPY_TRY(upload_chunk_table(&ct, base, stream));
+  float* v32 = (float*)(base + off_vals);
+  LAPY_TRY(cast_f64_f32(nnz, vals, v32, stream));
+  SellMatrix<float> sm;
+  bool fits = false;
+  LAPY_TRY(build_sell<float>(n, indptr, indices, v32, ct, base + off_sell, need - off_sell - 256, &sm, &fits, stream));
+  if (!fits) {
+    lapy_set_last_message("sell_f32_build: the padded matrix exceeds the reserved space");
+    return LAPY_ERR_WORKSPACE;
+  }
+  out->nunit = ct.nunit;
+  out->unit_row = ct.unit_row;
+  out->slice_ptr = sm.slice_ptr;
+  out->col = sm.col;
+  out->val = sm.val;
+  return LAPY_OK;
+}
+
+extern "C" int lapy_sell_f32_spmm(const lapy_sell_f32* m, int ncol, const float* x, float* y, void* stream_) {
+  using namespace lapy;
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (!m || !m->slice_ptr || !m->col || !m->val || !m->unit_row || m->nunit <= 0 || !x || !y) {
+    lapy_set_last_message("sell_f32_spmm: invalid arguments");
+    return LAPY_ERR_INVALID;
+  }
+  SellMatrix<float> sm;
+  sm.slice_ptr = m->slice_ptr;
+  sm.col = m->col;
+  sm.val = m->val;
+  switch (ncol) {
+    case 1: return launch_sell_pipe<1>(sm, m->unit_row, m->nunit, x, y, stream);
+    case 2: return launch_sell_pipe<2>(sm, m->unit_row, m->nunit, x, y, stream);
+    case 4: return launch_sell_pipe<4>(sm, m->unit_row, m->nunit, x, y, stream);
+    case 8: return launch_sell_pipe<8>(sm, m->unit_row, m->nunit, x, y, stream);
+    default:
+      lapy_set_last_message("sell_f32_spmm: ncol %d not in {1, 2, 4, 8}", ncol);
+      return LAPY_ERR_INVALID;
+  }
+}
 
 // Consistency of the persistent PCG's warp plan for the given segments (host
 // only, no device work): every virtual warp and virtual CTA holds at least one

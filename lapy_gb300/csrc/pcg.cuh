@@ -15,6 +15,7 @@ namespace lapy {
 // pieces  a virtual warp's unit range cut at segment boundaries; every piece
 //         owns one partial-sum slot, so a segment's dot products are the sum
 //         of its (few) pieces' partials, in a fixed order
+constexpr int kChunkScratch = 16;  // partial sums per chunk (columns of a segmented dot product)
 struct ChunkTable {
   int nseg = 0;
   int nchunk = 0;
@@ -22,6 +23,7 @@ struct ChunkTable {
   int32_t* chunk_seg = nullptr;  // device, nchunk
   int32_t* seg_chunk = nullptr;  // device, nseg + 1
   int32_t* seg_row = nullptr;    // device, nseg + 1
+  double* scratch = nullptr;     // device, nchunk * kChunkScratch: per-chunk partial sums
   int nunit = 0, npiece = 0, nvw = 0;
   int32_t* unit_row = nullptr;    // device, nunit + 1
   int32_t* piece_unit = nullptr;  // device, npiece + 1

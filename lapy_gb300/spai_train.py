@@ -55,14 +55,16 @@ def train(n_meshes: int = 128, level: int = 6, systems: int = 4096, batch: int =
 
 
 def evaluate(net: SpaiNet, n_test: int = 16, level: int = 7, seed: int = 1, rtol: float = 1e-8,
-             batch: int = 64) -> dict:
+             batch: int = 64, cols: int = 1) -> dict:
     """Jacobi-PCG, IC(0)-PCG and learned-SPAI-PCG on held-out meshes, same
     right-hand sides and tolerance; the meshes are solved in block-diagonal
     batches of `batch` (times summed over batches, iteration counts and
-    residuals the largest over batches)."""
+    residuals the largest over batches).  `cols` right-hand-side columns per
+    mesh are solved together (one pass over the matrix and the factors serves
+    all of them, as for a Lanczos block)."""
     rng = np.random.default_rng(seed)
     ms = meshes.deformed_icospheres([level] * n_test, [50_000 + seed * 1_000_003 + i for i in range(n_test)])
-    out = {"meshes": n_test, "level": level, "rows": 0, "rtol": rtol, "batch": batch}
+    out = {"meshes": n_test, "level": level, "rows": 0, "rtol": rtol, "batch": batch, "cols": cols}
     acc = {}
     for g0 in range(0, n_test, batch):
         inp = BatchInput(ms[g0:g0 + batch])
@@ -71,7 +73,8 @@ def evaluate(net: SpaiNet, n_test: int = 16, level: int = 7, seed: int = 1, rtol
         for kind in ("heat", "shift"):
             t = 10 ** rng.uniform(-4, -1, nb) if kind == "heat" else None
             sysg = SpaiSystems(inp, kind, t=t)
-            b = torch.from_numpy(rng.standard_normal(sysg.n)).to("cuda")
+            shape = (sysg.n,) if cols == 1 else (sysg.n, cols)
+            b = torch.from_numpy(rng.standard_normal(shape)).to("cuda")
             sysg.solve(b, rtol=rtol)  # warm
             t0 = _sync_time()
             _, rj, itj = sysg.solve(b, rtol=rtol)
