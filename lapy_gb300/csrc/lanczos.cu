@@ -266,7 +266,7 @@ __device__ __forceinline__ void df_fma(float2 x, float2 y, float& sh, float& sl)
 // TN with the basis in double-float form (see gemm_tn_blk_kernel for the layout).
 template <int P, int JB>
 __global__ void __launch_bounds__(256) gemm_tn_df_kernel(const float2* __restrict__ X, int64_t bst, int nblk,
-                                                         const double* __restrict__ Y,
+                                                         const float2* __restrict__ Y,
                                                          const int32_t* __restrict__ chunk_row,
                                                          const int32_t* __restrict__ chunk_seg,
                                                          const int32_t* __restrict__ active,
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256) gemm_tn_df_kernel(const float2* __restric
     for (int64_t r = chunk_row[c] + threadIdx.x; r < r1; r += blockDim.x) {
       float2 y[P];
 #pragma unroll
-      for (int b = 0; b < P; ++b) y[b] = df_split(__ldg(Y + r * P + b));
+      for (int b = 0; b < P; ++b) y[b] = __ldg(Y + r * P + b);
 #pragma unroll
       for (int jj = 0; jj < JB; ++jj) {
         if (j0 + jj < nblk) {
@@ -339,7 +339,8 @@ __global__ void __launch_bounds__(256) gemm_nn_df_kernel(const float2* __restric
     float sh[P], sl[P];
 #pragma unroll
     for (int b = 0; b < P; ++b) { sh[b] = 0.f; sl[b] = 0.f; }
-    for (int j = 0; j < nblk; ++j) {
+#pragma unroll 2
+    for (int j = 0; j < nblk; ++j) {  // two blocks' loads in flight
       const float2* xr = X + (int64_t)j * bst + r * P;
       const float2* hj = hdf + j * P * P;
 #pragma unroll
@@ -832,7 +833,7 @@ struct EigPlan {
 struct EigPtrs {
   void* ct_mem; void* gt_mem;
   int32_t* diag_pos; double* k64; float* k32; double* dinv64; float* dinv32;
-  double* basis; float2* basis_df; double* Y; double* W; double* MW; float2* S_df; float2* X_df;
+  double* basis; float2* basis_df; double* Y; double* W; double* MW; float2* MW_df; float2* S_df; float2* X_df;
   void* ir_ws; size_t ir_bytes;
   void* sell_mem; size_t sell_bytes;
   void* sell64_mem; void* sellm_mem; size_t sell64_bytes;
@@ -886,6 +887,7 @@ static size_t layout_eig(const EigPlan& P, char* base, EigPtrs* q) {
   e.Y = (double*)take(8 * n * p);
   e.W = (double*)take(8 * n * p);
   e.MW = (double*)take(8 * n * p);
+  e.MW_df = (float2*)take(8 * n * p);
   e.ir_bytes = ir_workspace_bytes(n, p, P.ct, 1, P.precond, P.nagg_max);
   e.ir_ws = take(e.ir_bytes);
   e.tl_bytes = P.precond == kPrecTwoLevel ? two_level_bytes(n, P.ct.h_seg_row.data(), ns, P.ct.nvc) : 0;
@@ -994,9 +996,14 @@ struct EigOps {
   template <int PB, int JB>
   int gemm_tn_df_p(int nbasis, const double* Y, const int32_t* act) const {
     const int nblk = nbasis / PB;
+    // Y split into (hi, lo) pairs once, not once per basis-block CTA (the
+    // split is FP64 work, the slow pipe here)
+    const int64_t m = P.n * PB;
+    to_df_kernel<<<lapy_ceil_div(m, 256), 256, 0, st>>>(m, Y, e.MW_df);
+    LAPY_TRY(lapy_check_launch("to_df_kernel"));
     dim3 grid(P.gt.nchunk, lapy_ceil_div(nblk, JB));
-    gemm_tn_df_kernel<PB, JB><<<grid, 256, 0, st>>>(e.basis_df, P.n * PB, nblk, Y, P.gt.chunk_row, P.gt.chunk_seg,
-                                                    act, e.partial);
+    gemm_tn_df_kernel<PB, JB><<<grid, 256, 0, st>>>(e.basis_df, P.n * PB, nblk, e.MW_df, P.gt.chunk_row,
+                                                    P.gt.chunk_seg, act, e.partial);
     return lapy_check_launch("gemm_tn_df_kernel");
   }
   int cgs_tn(int nbasis, const double* MW, double* out, int64_t out_stride, int ldo, const int32_t* act) const {
