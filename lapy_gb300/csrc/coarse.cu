@@ -462,12 +462,17 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
 
   // coarse-solve tasks (up to kCoarseTaskRows coarse rows of one segment),
   // split over the virtual CTAs in contiguous ranges of about equal time.  A
-  // task's time (ns) is modelled as a fixed part (staging the segment's
-  // residual, three CTA barriers), a memory round trip per warp pass (each
-  // warp computes kCoarseRowsPerPass rows per pass) plus the 128-entry row
-  // groups it streams, and its BF16 bytes at a CTA's share of the HBM
-  // bandwidth; small segments are dominated by the fixed parts, which a
-  // byte count alone would miss.  The aggregates of a virtual CTA's tasks
+  // task's time (ns) is modelled as a fixed part (its descriptor loads), a
+  // latency per warp pass (each warp computes kCoarseRowsPerPass rows per
+  // pass) plus one per 128-entry row group the pass streams, and, for the
+  // first task of a segment, the staging of the segment's residual (three
+  // CTA barriers).  The constants are a non-negative least-squares fit of
+  // per-CTA busy times measured with device timers on 512 meshes (levels
+  // 3-6): the BF16 bytes themselves did not matter, the dependent round
+  // trips did, so small segments' tasks cost several times what their bytes
+  // suggest.  Tasks of 16 rows (one pass) keep the split fine-grained: with
+  // 32-row tasks one level-6 task was a fifth of a virtual CTA's share and
+  // the busiest CTA ran a third longer than the mean.  The aggregates of a virtual CTA's tasks
   // are also its share of the restriction, and the reduction slots of each
   // segment's coarse partial sums follow from that split.
   std::vector<int32_t> task_seg, task_g0, task_g1;
@@ -482,8 +487,8 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
       const double passes = (double)((rows + kWarpsPerCta * kCoarseRowsPerPass - 1) /
                                      (kWarpsPerCta * kCoarseRowsPerPass));
       const double groups = (double)((pad8(nc[s]) + 127) / 128);
-      task_cost.push_back(1200.0 + passes * (800.0 + 250.0 * groups) +
-                          2.0 * rows * (double)pad8(nc[s]) / 8.7);
+      const bool first = g == seg_agg[s];
+      task_cost.push_back(1900.0 + (first ? 1600.0 : 0.0) + passes * (800.0 + 800.0 * groups));
     }
   const int ntask = (int)task_seg.size();
   std::vector<int32_t> vc_task(nvc + 1, 0);

@@ -1245,8 +1245,6 @@ static int eigs_run(const EigPlan& P, const EigPtrs& e, const int32_t* indptr, c
     // product: a first pass, then a second one where the first cancelled
     // much of a column (the mask leaves H = 0 for the other segments)
     const int nbasis = (j + 1) * p;
-    BMat Qm{e.basis, p, n * p};
-    BMat MWm{e.MW, p, 0};
     LAPY_TRY(ops.apply_M(e.W, e.MW, p));
     LAPY_TRY(seg_col_dot(e.W, e.MW, p, P.ct, e.wn0, st));
     LAPY_TRY(ops.cgs_tn(nbasis, e.MW, e.Hsum, (int64_t)lda * p, p, e.active));

@@ -646,20 +646,20 @@ __device__ __forceinline__ void coarse_restrict(const PcgArgs<V>& a, const int32
   FOR_MY_AGGS(a, {
     if (!all) {
       bool act = false;
-#pragma unroll
+_Pragma("unroll")
       for (int q = 0; q < NP; ++q) act |= st[s * NP + q] == kActive;
       if (!act) continue;
     }
     S acc[NP];
-#pragma unroll
+_Pragma("unroll")
     for (int q = 0; q < NP; ++q) acc[q] = S(0);
     for (int32_t m = a.pc.agg_ptr[g] + lane; m < a.pc.agg_ptr[g + 1]; m += 32) {
       V r[NP];
       load_row<V, NP>(a.R, a.pc.agg_contig ? m : a.pc.agg_row[m], r);
-#pragma unroll
+_Pragma("unroll")
       for (int q = 0; q < NP; ++q) acc[q] += (S)r[q];
     }
-#pragma unroll
+_Pragma("unroll")
     for (int q = 0; q < NP; ++q) {
       const S v = warp_sum(acc[q]);
       if (lane == q) a.rc[(int64_t)g * NP + q] = v;
@@ -852,9 +852,17 @@ __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t*
       const int g0 = a.pc.task_g0[t], g1 = a.pc.task_g1[t];
       const float c = a.pc.kscale[s];
       if (threadIdx.x == 0) cbytes += 2ull * (unsigned long long)(g1 - g0) * (unsigned long long)ld;
+      const uint16_t* kseg = a.pc.kinv + a.pc.kinv_off[s];
       for (int r0 = g0 + warp * RW; r0 < g1; r0 += kWarps * RW) {
         const int nr = min(RW, g1 - r0);
-        const uint16_t* kr = a.pc.kinv + a.pc.kinv_off[s] + (int64_t)(r0 - base) * ld;
+        const uint16_t* kr = kseg + (int64_t)(r0 - base) * ld;
+        // the epilogue's operands of the lane that writes (row r0 + lane / NP,
+        // column lane % NP), loaded before the row stream so that their round
+        // trip overlaps it
+        const int my_r = lane / NP;
+        const bool my_ok = lane < RW * NP && my_r < nr;
+        const float my_rc = my_ok ? a.rc[(int64_t)(r0 + my_r) * NP + lane % NP] : 0.f;
+        const float my_cv = my_ok ? c * vs[r0 + my_r - base] : 0.f;
         float acc[RW][NP];
 #pragma unroll
         for (int r = 0; r < RW; ++r)
@@ -880,13 +888,13 @@ __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t*
 #pragma unroll
         for (int r = 0; r < RW; ++r) {
           const int g = r0 + r;
-          const float cv = (r < nr) ? c * vs[g - base] : 0.f;
 #pragma unroll
           for (int q = 0; q < NP; ++q) {
-            const float y = warp_sum(acc[r][q]) + cv * vrc[q];
+            const float sum = warp_sum(acc[r][q]);
             if (r < nr && lane == r * NP + q) {
+              const float y = sum + my_cv * vrc[q];
               a.yc[(int64_t)g * NP + q] = y;
-              a.csl[(int64_t)g * NP + q] = y * a.rc[(int64_t)g * NP + q];
+              a.csl[(int64_t)g * NP + q] = y * my_rc;
             }
           }
         }

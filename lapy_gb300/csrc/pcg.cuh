@@ -56,7 +56,7 @@ enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1, kPrecTwoLevel = 2, kPrecIC
 
 // Coarse rows per coarse-solve task: 8 warps x 4 rows; a warp computes
 // kCoarseRowsPerPass of them at a time (block widths up to 4).
-constexpr int kCoarseTaskRows = 32;
+constexpr int kCoarseTaskRows = 16;
 constexpr int kWarpsPerCta = 8;
 #ifndef LAPY_COARSE_RW
 #define LAPY_COARSE_RW 2
