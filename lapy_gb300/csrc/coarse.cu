@@ -62,7 +62,7 @@ size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg, int nvc) {
          a256(4 * (size_t)(nseg + 1)) + a256(8 * (size_t)(nseg + 1)) + a256(2 * (size_t)ne_pad) +
          2 * a256(8 * (size_t)ne) + a256(4 * (size_t)nseg) + a256(4 * (size_t)(std::max(nvc, 1) + 1)) * 2 +
          a256(4 * (size_t)(nseg + 1)) + a256(4 * (size_t)std::max(nseg, 1)) + a256(4 * (size_t)na) +
-         a256(4 * (size_t)std::max(nseg, 1)) + 3 * a256(4 * (size_t)std::max<int64_t>(nt, 1)) +
+         a256(4 * (size_t)std::max(nseg, 1)) + 5 * a256(4 * (size_t)std::max<int64_t>(nt, 1)) +
          a256(8 * (size_t)(nseg + 1)) + 2048;
 }
 
@@ -491,6 +491,31 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
       task_cost.push_back(1900.0 + (first ? 1600.0 : 0.0) + passes * (800.0 + 800.0 * groups));
     }
   const int ntask = (int)task_seg.size();
+  // groups of up to kCoarseGroupTasks consecutive tasks of one segment, in
+  // decreasing order of modelled cost (the cheap groups of small segments
+  // last, where they even out the CTAs' finishing times)
+  std::vector<int32_t> grp_t0, grp_t1;
+  {
+    std::vector<std::pair<double, int>> order;
+    std::vector<int32_t> g0v, g1v;
+    for (int t = 0; t < ntask;) {
+      int t1 = t + 1;
+      while (t1 < ntask && t1 - t < kCoarseGroupTasks && task_seg[t1] == task_seg[t]) ++t1;
+      double c = 0.0;
+      for (int q = t; q < t1; ++q) c += task_cost[q];
+      order.push_back({-c, (int)g0v.size()});
+      g0v.push_back(t);
+      g1v.push_back(t1);
+      t = t1;
+    }
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<double, int>& x, const std::pair<double, int>& y) { return x.first < y.first; });
+    for (const auto& o : order) {
+      grp_t0.push_back(g0v[o.second]);
+      grp_t1.push_back(g1v[o.second]);
+    }
+  }
+  const int ngroup = (int)grp_t0.size();
   std::vector<int32_t> vc_task(nvc + 1, 0);
   {
     double total = 0.0;
@@ -546,6 +571,8 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   int32_t* d_tg0 = (int32_t*)w; w += a256(4 * (size_t)std::max<int64_t>(nt_max, 1));
   int32_t* d_tg1 = (int32_t*)w; w += a256(4 * (size_t)std::max<int64_t>(nt_max, 1));
   int32_t* d_vct = (int32_t*)w; w += a256(4 * (size_t)(nvc + 1));
+  int32_t* d_gt0 = (int32_t*)w; w += a256(4 * (size_t)std::max<int64_t>(nt_max, 1));
+  int32_t* d_gt1 = (int32_t*)w; w += a256(4 * (size_t)std::max<int64_t>(nt_max, 1));
   int64_t* d_offp = (int64_t*)w; w += a256(8 * (size_t)(nseg + 1));
   int* d_fail = (int*)w;
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_agg, agg.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, stream));
@@ -565,6 +592,10 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
     LAPY_CUDA_TRY(cudaMemcpyAsync(d_tg1, task_g1.data(), 4 * (size_t)ntask, cudaMemcpyHostToDevice, stream));
   }
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_vct, vc_task.data(), 4 * vc_task.size(), cudaMemcpyHostToDevice, stream));
+  if (ngroup > 0) {
+    LAPY_CUDA_TRY(cudaMemcpyAsync(d_gt0, grp_t0.data(), 4 * (size_t)ngroup, cudaMemcpyHostToDevice, stream));
+    LAPY_CUDA_TRY(cudaMemcpyAsync(d_gt1, grp_t1.data(), 4 * (size_t)ngroup, cudaMemcpyHostToDevice, stream));
+  }
   LAPY_CUDA_TRY(cudaMemcpyAsync(d_offp, off_pad.data(), 8 * off_pad.size(), cudaMemcpyHostToDevice, stream));
   if (off[nseg] > 0) LAPY_CUDA_TRY(cudaMemsetAsync(d_kc, 0, 8 * (size_t)off[nseg], stream));
   LAPY_CUDA_TRY(cudaMemsetAsync(d_fail, 0, 4 * (size_t)nseg, stream));
@@ -595,6 +626,9 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
   pc->task_g0 = d_tg0;
   pc->task_g1 = d_tg1;
   pc->vc_task = d_vct;
+  pc->ngroup = ngroup;
+  pc->grp_t0 = d_gt0;
+  pc->grp_t1 = d_gt1;
   pc->nvc = nvc;
   pc->naslot = seg_aslot[nseg];
   pc->max_seg_agg = nseg > 0 ? *std::max_element(nc.begin(), nc.end()) : 0;

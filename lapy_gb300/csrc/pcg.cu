@@ -204,6 +204,7 @@ struct PcgArgs {
   S* csl;             // [nagg][NP] rc .* yc (coarse part of r'z)
   S* rc_part;         // [2][npiece][NP] partial rc of aggregates that straddle pieces
   int32_t* rc_cnt;    // [nagg] arrivals at a straddling aggregate (zero between phases)
+  unsigned* cq;       // [2] coarse task-group counters, used by alternate coarse phases
   S* rz;              // [2][nseg][NP]
   S* bb;              // [nseg][NP]
   int32_t* state;     // [2][nseg][NP]
@@ -727,7 +728,8 @@ __device__ __forceinline__ float bf16x4_elem(const uint2& w, int e) {
 // over j < jend (a multiple of 4), for the nr <= RW rows starting at kr (row
 // stride ld, a multiple of 8).  Lane l streams entries 4l .. 4l+3 of every
 // 128, one 8-byte load per row, the next group's loads issued before the
-// current group is used (two groups of RW loads in flight per lane); each x
+// current group is used (two groups of RW loads in flight per lane; a third
+// measured no faster and spilled more); each x
 // value read serves RW rows.  SWZ: x is the staged copy in shared memory,
 // entry j at (j % 4) * (ld / 4) + j / 4, so that the 32 lanes read 32
 // consecutive entries (no bank conflicts); otherwise x is rc in global
@@ -772,7 +774,7 @@ __device__ __forceinline__ void coarse_rows(const uint16_t* __restrict__ kr, int
 // below nc) and forms v'rc itself.
 template <typename V, int NP>
 __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t* st, bool all, float* stage,
-                                             int stage_floats, unsigned long long& cbytes) {
+                                             int stage_floats, unsigned long long& cbytes, unsigned* ctr) {
   static_assert(sizeof(V) == 4, "the two-level preconditioner runs FP32 iterations");
   // rows per warp pass (each staged residual value read from shared memory
   // serves that many rows; bounded by the 48-register budget)
@@ -781,9 +783,30 @@ __device__ __forceinline__ void coarse_solve(const PcgArgs<V>& a, const int32_t*
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __shared__ float s_vrc[NP];
   __shared__ float s_red[kWarps][NP];
+  __shared__ int s_grab;
   int staged = -1;
-  for (int vc = blockIdx.x; vc < a.pc.nvc; vc += gridDim.x) {
-    for (int t = a.pc.vc_task[vc]; t < a.pc.vc_task[vc + 1]; ++t) {
+  // task ranges: groups taken from the counter (every CTA until the list is
+  // exhausted), or the CTA's virtual CTAs' static ranges when the launch
+  // folds partial sums per virtual CTA
+  const bool dyn = !a.fold && a.pc.ngroup > 0;
+  int vc = blockIdx.x;
+  for (;;) {
+    int t0, t1;
+    if (dyn) {
+      if (threadIdx.x == 0) s_grab = (int)atomicAdd(ctr, 1u);
+      __syncthreads();
+      const int gi = s_grab;
+      __syncthreads();  // every thread has read s_grab before it changes
+      if (gi >= a.pc.ngroup) break;
+      t0 = a.pc.grp_t0[gi];
+      t1 = a.pc.grp_t1[gi];
+    } else {
+      if (vc >= a.pc.nvc) break;
+      t0 = a.pc.vc_task[vc];
+      t1 = a.pc.vc_task[vc + 1];
+      vc += gridDim.x;
+    }
+    for (int t = t0; t < t1; ++t) {
       const int s = a.pc.task_seg[t];
       if (!all) {
         bool act = false;
@@ -1137,7 +1160,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     if (!grid_sync(a.bar)) return;
     coarse_restrict<V, NP>(a, nullptr, true);
     if (!grid_sync(a.bar)) return;
-    coarse_solve<V, NP>(a, nullptr, true, reinterpret_cast<float*>(stage_raw), kStageBytes / 4, c_bytes);
+    coarse_solve<V, NP>(a, nullptr, true, reinterpret_cast<float*>(stage_raw), kStageBytes / 4, c_bytes, a.cq);
   }
   if constexpr (PC == kPrecIC0) {  // Z = (L L')^-1 R, r'z; P = Z below
     if (!grid_sync(a.bar)) return;
@@ -1169,6 +1192,8 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     }
   }
   if (!grid_sync(a.bar)) return;
+  // the first iteration's coarse phase takes groups from counter 1
+  if (PC == kPrecTwoLevel && blockIdx.x == 0 && threadIdx.x == 0) a.cq[1] = 0u;
   // ---- segment initialisation (the warp holding a segment's first piece publishes)
   FOR_MY_PIECES(a, {
     if constexpr (PC == kPrecFactored) {
@@ -1515,7 +1540,10 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
         if (!grid_sync(a.bar)) return;
       }
       mark(3);
-      coarse_solve<V, NP>(a, st_cur, false, reinterpret_cast<float*>(stage_raw), kStageBytes / 4, c_bytes);
+      // coarse phase k = it + 1 takes groups from counter k % 2; the other
+      // one is cleared in the direction phase for phase k + 1
+      coarse_solve<V, NP>(a, st_cur, false, reinterpret_cast<float*>(stage_raw), kStageBytes / 4, c_bytes,
+                          a.cq + ((it + 1) & 1));
       if (!grid_sync(a.bar)) return;
       mark(4);
     }
@@ -1559,6 +1587,7 @@ __global__ void __launch_bounds__(kPcgThreads, kPlanCtasPerSm) pcg_kernel(PcgArg
     }
 
     // ---- phase C: convergence, beta, P = Z + beta P
+    if (PC == kPrecTwoLevel && blockIdx.x == 0 && threadIdx.x == 0) a.cq[it & 1] = 0u;
     FOR_MY_PIECES(a, {
       S pq[NP], rzn[NP], rr[NP];
       piece_totals<V, NP>(a, part_pq, slot_pq, s, pq);
@@ -1890,7 +1919,8 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.state = (int32_t*)w; w += a256(sizeof(int32_t) * 2 * (size_t)ct.nseg * p);
   // control words: [2] iters, [5] err, [6..9] work (u64 x2), [10..11] ru_flag,
   // [12] updates, [14..27] phase times (u64 x kPcgPhases), [28..29] coarse
-  // bytes (u64); the barrier word sits alone on the next 128-byte line
+  // bytes (u64), [30..31] coarse task-group counters; the barrier word sits
+  // alone on the next 128-byte line
   static_assert(14 + 2 * kPcgPhases <= 28, "phase timers overlap the coarse byte counter");
   unsigned* ctl = (unsigned*)w;
   w += a256(256);
@@ -1901,6 +1931,7 @@ static int pcg_run(int64_t n, const int32_t* indptr, const int32_t* indices, con
   a.ru_flag = ctl + 10;
   a.n_updates = ctl + 12;
   a.cwork = (unsigned long long*)(ctl + 28);
+  a.cq = ctl + 30;
   a.part64 = (double*)w; w += a256(sizeof(double) * (size_t)ct.npiece * p);
   a.slot64 = (double*)w; w += a256(sizeof(double) * (size_t)ct.nslot * p);
   a.rref = (S*)w; w += a256(sizeof(double) * (size_t)ct.nseg * p);

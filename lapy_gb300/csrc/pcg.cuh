@@ -57,6 +57,7 @@ enum PcgPrecond { kPrecJacobi = 0, kPrecFactored = 1, kPrecTwoLevel = 2, kPrecIC
 // Coarse rows per coarse-solve task: 8 warps x 4 rows; a warp computes
 // kCoarseRowsPerPass of them at a time (block widths up to 4).
 constexpr int kCoarseTaskRows = 16;
+constexpr int kCoarseGroupTasks = 4;  // tasks per dynamically scheduled group (one staging)
 constexpr int kWarpsPerCta = 8;
 #ifndef LAPY_COARSE_RW
 #define LAPY_COARSE_RW 2
@@ -134,6 +135,12 @@ struct PcgPrecondDesc {
   const int32_t* task_g0 = nullptr;   // ntask
   const int32_t* task_g1 = nullptr;   // ntask
   const int32_t* vc_task = nullptr;   // nvc + 1
+  // Task groups for dynamic scheduling (launches without reduction slots):
+  // up to kCoarseGroupTasks consecutive tasks of one segment, listed by
+  // decreasing modelled cost; CTAs take the next group from a counter.
+  int ngroup = 0;
+  const int32_t* grp_t0 = nullptr;    // ngroup: first task
+  const int32_t* grp_t1 = nullptr;    // ngroup: one past the last task
   // coarse work split over the PCG's virtual CTAs: aggregates
   // [vc_agg[v], vc_agg[v+1]) (contiguous, about equal cost) go to virtual
   // CTA v; segment s owns the reduction slots [seg_aslot[s], seg_aslot[s+1])
