@@ -371,6 +371,8 @@ def run_gpu(args, rank, world):
     }
     if not args.no_spmm:
         line["spmm"] = run_spmm(batch_in, hbm, peak_kind)
+    if not args.no_c1:
+        line["c1"] = run_c1(args, with_cpu=rank == 0 and not args.no_cpu)
     heat_x = None
     if not args.no_heat:
         line["heat"], heat_x = run_heat(args, meshes, lv, batch_in, world)
@@ -402,6 +404,44 @@ def _timed(fn, steps, warmup):
     ev1.record()
     torch.cuda.synchronize()
     return ev0.elapsed_time(ev1) / 1e3
+
+
+def run_c1(args, with_cpu, reps=5, warmup=2):
+    """The single-mesh latency configuration inside the default line: icosphere
+    L5 (10,242 vertices), Solver(mesh).eigs(50) from host arrays each call
+    (upload, assembly, eigensolve, download), the FP64 certificate of the last
+    call, and the reference method on one host core for the same mesh."""
+    import torch
+
+    from lapy_gb300 import Solver, TriaMesh, meshes
+
+    mesh0 = meshes.icosphere(5)
+    info = {}
+
+    def call():
+        fem = Solver(TriaMesh(mesh0.v.copy(), mesh0.t.copy()), lump=False)
+        info["ev"], info["X"] = fem.eigs(k=50)
+        info["fem"] = fem
+        torch.cuda.synchronize()
+
+    for _ in range(warmup):
+        call()
+    secs = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        call()
+        secs.append(time.perf_counter() - t0)
+    med = float(np.median(secs))
+    out = {"workload": "icosphere L5 (10,242 vertices), Solver(mesh).eigs(50) from host arrays",
+           "value": 1.0 / med, "unit": "spectra/s", "seconds_median": med, "seconds": secs,
+           "certificate": eig_certificate(info["fem"], info["ev"], info["X"])}
+    if with_cpu:
+        cpu, ref = cpu_single("sphere-l5", mesh0, args.seed, args.cpu_timeout)
+        out["cpu_baseline"] = cpu
+        if ref is not None and "ev" in ref:
+            out["accuracy"] = eig_accuracy(np.asarray(info["ev"])[None, :], [0], [ref["ev"]])
+            out["vs_cpu_one_core"] = cpu["seconds"] / med
+    return out
 
 
 def run_spmm(batch_in, hbm, peak_kind, reps=20, warmup=3):
@@ -779,6 +819,7 @@ def main():
     ap.add_argument("--cpu-timeout", type=float, default=600.0, help="single-mesh workloads: CPU run time limit (s)")
     ap.add_argument("--no-heat", action="store_true")
     ap.add_argument("--no-spmm", action="store_true", help="skip the standalone SELL SpMM leg")
+    ap.add_argument("--no-c1", action="store_true", help="skip the single-mesh (icosphere L5) leg")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-test", type=int, default=32, help="held-out level-7 meshes of the learned-SPAI leg")
