@@ -62,22 +62,26 @@ __global__ void __launch_bounds__(256) chunk_col_dot_kernel(const double* __rest
   }
 }
 
+// One warp per (segment, column): lane l adds chunks l, l + 32, ... of the
+// segment, then a butterfly sum (a fixed order for a given chunk count).
 __global__ void seg_sum_chunks_kernel(int nseg, int ncol, const int32_t* __restrict__ seg_chunk,
                                       const double* __restrict__ part, double* __restrict__ out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (t >= nseg * ncol) return;
   const int s = t / ncol, q = t - s * ncol;
   double acc = 0.0;
-  for (int k = seg_chunk[s]; k < seg_chunk[s + 1]; ++k) acc += part[(int64_t)k * kChunkScratch + q];
-  out[t] = acc;
+  for (int k = seg_chunk[s] + lane; k < seg_chunk[s + 1]; k += 32) acc += part[(int64_t)k * kChunkScratch + q];
+  acc = warp_sum(acc);
+  if (lane == 0) out[t] = acc;
 }
 
 template <int NC>
 static int chunked_dot(const double* x, const double* y, const ChunkTable& ct, double* out, cudaStream_t stream) {
   chunk_col_dot_kernel<NC><<<ct.nchunk, 256, 0, stream>>>(x, y, ct.chunk_row, ct.scratch);
   LAPY_TRY(lapy_check_launch("chunk_col_dot_kernel"));
-  seg_sum_chunks_kernel<<<lapy_ceil_div(ct.nseg * NC, 128), 128, 0, stream>>>(ct.nseg, NC, ct.seg_chunk, ct.scratch,
-                                                                              out);
+  seg_sum_chunks_kernel<<<lapy_ceil_div((int64_t)ct.nseg * NC * 32, 128), 128, 0, stream>>>(ct.nseg, NC, ct.seg_chunk,
+                                                                                           ct.scratch, out);
   return lapy_check_launch("seg_sum_chunks_kernel");
 }
 

@@ -174,7 +174,7 @@ __global__ void coarse_galerkin_kernel(int nagg, const int32_t* __restrict__ agg
   }
 }
 
-constexpr int kInvThreads = 512;
+constexpr int kInvThreads = 1024;
 // Power iterations for the dominant eigenvector of the coarse inverse: the
 // smallest eigenvalue of W'KW is the shifted constant mode, separated from
 // the next by two to four orders of magnitude on mesh systems, so a few
