@@ -147,7 +147,11 @@ int lapy_csr_pattern_map(int64_t n, const int32_t* a_indptr, const int32_t* a_in
 /* Batch construction (the reference handles one mesh per call; a batch of
  * meshes is concatenated into one block-diagonal system).
  * lapy_h2d_concat: `count` host buffers (src[i], bytes[i]) copied back to
- * back into the device buffer dst, in order, on `stream`.
+ * back into the device buffer dst, in order, on `stream`.  With a pinned
+ * host buffer of at least the total size (`pinned`, `pinned_bytes`; may be
+ * null), the buffers are first gathered into it on a few host threads and
+ * copied with one transfer; it must stay untouched until the copy on
+ * `stream` has completed.  Without one, each buffer is its own copy.
  * lapy_seg_offset_elements: t_out (device, m x npe int32) = t_in (device, the
  * meshes' own vertex indices concatenated; int64 if idx64 else int32) +
  * seg_row[s] for the elements [seg_elem[s], seg_elem[s+1]) of mesh s
@@ -157,7 +161,8 @@ int lapy_csr_pattern_map(int64_t n, const int32_t* a_indptr, const int32_t* a_in
  * lapy_seg_unit_vector: out (device, n) = the indicator of vertex vid[s] of
  * every mesh s (the right-hand sides of heat.diffusion, lapy/heat.py:215-221,
  * for one seed vertex per mesh). */
-int lapy_h2d_concat(int count, const void* const* src, const size_t* bytes, void* dst, void* stream);
+int lapy_h2d_concat(int count, const void* const* src, const size_t* bytes, void* dst, void* pinned,
+                    size_t pinned_bytes, void* stream);
 int lapy_seg_offset_elements(int64_t m, int npe, int nseg, const int32_t* seg_elem,
                              const int32_t* seg_row, const void* t_in, int idx64, int32_t* t_out,
                              int32_t* seg_max, void* stream);

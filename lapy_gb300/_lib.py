@@ -82,7 +82,7 @@ _SIGNATURES = {
     "lapy_fem_batch_numeric_workspace_bytes": (_sz, [_i64, _int, _int]),
     "lapy_fem_batch_numeric": (_int, [_int, _vp, _int, _vp, _i64, _int, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _int,
                                       _int, _vp, _vp, _vp, _sz, _vp]),
-    "lapy_h2d_concat": (_int, [_int, C.POINTER(_vp), C.POINTER(_sz), _vp, _vp]),
+    "lapy_h2d_concat": (_int, [_int, C.POINTER(_vp), C.POINTER(_sz), _vp, _vp, _sz, _vp]),
     "lapy_seg_offset_elements": (_int, [_i64, _int, _int, _vp, _vp, _vp, _int, _vp, _vp, _vp]),
     "lapy_seg_unit_vector": (_int, [_i64, _int, _vp, _vp, _vp, _vp]),
     "lapy_csr_diag_index": (_int, [_i64, _vp, _vp, _vp, _vp]),

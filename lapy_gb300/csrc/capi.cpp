@@ -5,6 +5,9 @@
 #include <string.h>
 #include <atomic>
 #include <mutex>
+#include <algorithm>
+#include <cstring>
+#include <thread>
 #include <vector>
 #include "lapy_gb300.h"
 
@@ -126,19 +129,50 @@ extern "C" const char* lapy_last_error(void) { return g_last_error; }
 
 // Host buffers copied back to back into one device buffer (one
 // cudaMemcpyAsync per buffer, in order).
-extern "C" int lapy_h2d_concat(int count, const void* const* src, const size_t* bytes, void* dst, void* stream) {
+extern "C" int lapy_h2d_concat(int count, const void* const* src, const size_t* bytes, void* dst, void* pinned,
+                               size_t pinned_bytes, void* stream) {
   if (count < 0 || (count > 0 && (!src || !bytes || !dst))) return LAPY_ERR_INVALID;
-  size_t off = 0;
+  size_t total = 0;
+  for (int i = 0; i < count; ++i) {
+    if (bytes[i] != 0 && !src[i]) return LAPY_ERR_INVALID;
+    total += bytes[i];
+  }
+  if (total == 0) return LAPY_OK;
+  if (pinned && pinned_bytes >= total) {
+    // gather into the pinned buffer on a few host threads (contiguous runs
+    // of buffers of about equal size), then one copy
+    std::vector<size_t> off(count + 1, 0);
+    for (int i = 0; i < count; ++i) off[i + 1] = off[i] + bytes[i];
+    const int nthr = (int)std::max<size_t>(1, std::min<size_t>({8, (size_t)std::max(1u, std::thread::hardware_concurrency()),
+                                                                  total / (4u << 20) + 1}));
+    auto work = [&](int t) {
+      const size_t lo = total * t / nthr, hi = total * (t + 1) / nthr;
+      for (int i = 0; i < count; ++i) {
+        const size_t a = std::max(lo, off[i]), b = std::min(hi, off[i + 1]);
+        if (a < b) std::memcpy((char*)pinned + a, (const char*)src[i] + (a - off[i]), b - a);
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthr; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool) th.join();
+    const cudaError_t e = cudaMemcpyAsync(dst, pinned, total, cudaMemcpyHostToDevice, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+      lapy_set_last_cuda_error(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+      return LAPY_ERR_CUDA;
+    }
+    return LAPY_OK;
+  }
+  size_t o = 0;
   for (int i = 0; i < count; ++i) {
     if (bytes[i] == 0) continue;
-    if (!src[i]) return LAPY_ERR_INVALID;
-    const cudaError_t e = cudaMemcpyAsync((char*)dst + off, src[i], bytes[i], cudaMemcpyHostToDevice,
+    const cudaError_t e = cudaMemcpyAsync((char*)dst + o, src[i], bytes[i], cudaMemcpyHostToDevice,
                                           (cudaStream_t)stream);
     if (e != cudaSuccess) {
       lapy_set_last_cuda_error(e, "cudaMemcpyAsync", __FILE__, __LINE__);
       return LAPY_ERR_CUDA;
     }
-    off += bytes[i];
+    o += bytes[i];
   }
   return LAPY_OK;
 }

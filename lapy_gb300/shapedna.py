@@ -113,18 +113,26 @@ class BatchInput:
         ts = [np.ascontiguousarray(t, dtype=np.int64 if idx64 else np.int32) for t in ts]
         n, m_tot, nseg = seg[-1], segel[-1], len(meshes)
         s = stream()
+        # the meshes' arrays are gathered into one pinned host buffer (by the
+        # library, on a few host threads) and sent with one copy per array
+        # kind: many small copies from pageable memory were several times
+        # slower, and their cost varied from call to call
+        vbytes = sum(a.nbytes for a in vs)
+        tbytes = sum(a.nbytes for a in ts)
+        pinned = torch.empty(vbytes + tbytes, dtype=torch.uint8, pin_memory=True)
 
-        def upload(arrays, out):
+        def upload(arrays, out, off, nbytes):
             ptrs = (C.c_void_p * len(arrays))(*[a.ctypes.data for a in arrays])
             sizes = (C.c_size_t * len(arrays))(*[a.nbytes for a in arrays])
-            _lib.check(L.lapy_h2d_concat(len(arrays), ptrs, sizes, dptr(out), s), "h2d_concat")
+            _lib.check(L.lapy_h2d_concat(len(arrays), ptrs, sizes, dptr(out), pinned.data_ptr() + off, nbytes, s),
+                       "h2d_concat")
 
-        # every mesh's arrays straight into the device buffers; the element
-        # indices are offset (and checked) on the device
+        # every mesh's arrays into the device buffers; the element indices are
+        # offset (and checked) on the device
         v = torch.empty((n, 3), dtype=torch.float32 if f32 else torch.float64, device="cuda")
-        upload(vs, v)
+        upload(vs, v, 0, vbytes)
         traw = torch.empty((m_tot, npe), dtype=torch.int64 if idx64 else torch.int32, device="cuda")
-        upload(ts, traw)
+        upload(ts, traw, vbytes, tbytes)
         self.seg_row = np.array(seg, dtype=np.int32)
         self.seg_elem = np.array(segel, dtype=np.int32)
         self.seg_row_dev = torch.from_numpy(self.seg_row).to("cuda")
@@ -133,7 +141,8 @@ class BatchInput:
         segmax = torch.empty(nseg + 1, dtype=torch.int32, device="cuda")
         _lib.check(L.lapy_seg_offset_elements(m_tot, npe, nseg, dptr(self.seg_elem_dev), dptr(self.seg_row_dev),
                                               dptr(traw), int(idx64), dptr(t), dptr(segmax), s), "seg_offset_elements")
-        sm = segmax.cpu().numpy()
+        sm = segmax.cpu().numpy()  # also the end of the copies out of `pinned`
+        del pinned
         if sm[nseg] != 0:
             raise ValueError("element indices outside their mesh's vertices")
         if np.any(sm[:nseg] + 1 != np.diff(self.seg_row)):
