@@ -1011,7 +1011,7 @@ struct EigOps {
     int st_ = LAPY_ERR_INVALID;
     if (p == 1) st_ = gemm_tn_df_p<1, 16>(nbasis, MW, act);
     else if (p == 2) st_ = gemm_tn_df_p<2, 8>(nbasis, MW, act);
-    else if (p == 4) st_ = gemm_tn_df_p<4, 2>(nbasis, MW, act);
+    else if (p == 4) st_ = gemm_tn_df_p<4, 1>(nbasis, MW, act);
     else if (p == 8) st_ = gemm_tn_df_p<8, 1>(nbasis, MW, act);
     else return gemm_tn(BMat{e.basis, p, P.n * p}, nbasis, BMat{MW, p, 0}, p, out, out_stride, ldo, act);
     LAPY_TRY(st_);
