@@ -1019,12 +1019,14 @@ struct EigOps {
     gemm_tn_reduce_kernel<<<g2, 256, 0, st>>>(e.partial, nbasis, p, P.gt.seg_chunk, out, out_stride, ldo);
     return lapy_check_launch("gemm_tn_reduce_kernel");
   }
+  // (on the PCG's short chunks: the NN product has no per-chunk reduction,
+  // and the long basis-product chunks left half the SMs' warp slots empty)
   template <int PB>
   int gemm_nn_df_p(int nbasis, const double* H, int64_t hs, int ldh, double* W, const int32_t* act) const {
     const int nblk = nbasis / PB;
     const size_t smem = sizeof(float2) * (size_t)nblk * PB * PB;
-    gemm_nn_df_kernel<PB><<<P.gt.nchunk, 256, smem, st>>>(e.basis_df, P.n * PB, nblk, H, hs, ldh, W, -1.0, 1.0,
-                                                          P.gt.chunk_row, P.gt.chunk_seg, act);
+    gemm_nn_df_kernel<PB><<<P.ct.nchunk, 256, smem, st>>>(e.basis_df, P.n * PB, nblk, H, hs, ldh, W, -1.0, 1.0,
+                                                          P.ct.chunk_row, P.ct.chunk_seg, act);
     return lapy_check_launch("gemm_nn_df_kernel");
   }
   // W -= Q H per segment
