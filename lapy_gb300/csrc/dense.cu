@@ -15,6 +15,7 @@
 #include <cfloat>
 #include <cmath>
 #include "dense.cuh"
+#include "dfloat.cuh"
 
 namespace lapy {
 
@@ -119,12 +120,12 @@ __device__ void tri_solve(const double* U0i, const double* U1, const double* U2,
   }
 }
 
-__global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int lda,
+__global__ void __launch_bounds__(kEigThreads, 4) sym_eig_kernel(double* Aall, int lda,
                                                               const int32_t* nsize, int want,
                                                               double* theta_all, double* S_all,
                                                               double* work_all, size_t wstride,
                                                               const int32_t* active) {
-  extern __shared__ double svec[];  // v and w of the current reflector (2 lda)
+  extern __shared__ double svec[];  // v and w of the current reflector, FP64 and double-float (4 lda)
   __shared__ double sh[32];
   __shared__ double s_tau, s_beta, s_K;
   __shared__ int s_skip;
@@ -146,17 +147,28 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
   double* S = S_all + (int64_t)b * lda * want;
   const int nw = min(want, n);
 
-  // ---- 1. Householder tridiagonalisation (lower), A[i*lda + j]
+  // ---- 1. Householder tridiagonalisation (lower), A[i*lda + j].  The
+  // trailing block A22 is held in double-float (the 8 bytes of an entry as
+  // an FP32 pair): its product with the reflector and its rank-2 update, the
+  // O(n^3) part, run on the FP32 pipe, 64x the FP64 rate here; scalars,
+  // reflectors (written back as FP64 into row and column k) and the
+  // tridiagonal stay FP64.
+  float2* Af = reinterpret_cast<float2*>(A);
+  for (int64_t q = t; q < (int64_t)n * n; q += kEigThreads) {
+    const int64_t r = q / n, c = q - r * n;
+    Af[r * lda + c] = df_split(A[r * lda + c]);
+  }
+  __syncthreads();
   for (int k = 0; k < n - 2; ++k) {
     // column k below the subdiagonal
     double s2 = 0.0;
     for (int i = k + 2 + t; i < n; i += kEigThreads) {
-      const double x = A[(int64_t)i * lda + k];
+      const double x = df_to_double(Af[(int64_t)i * lda + k]);
       s2 += x * x;
     }
     s2 = block_sum(s2, sh);
     if (t == 0) {
-      const double alpha = A[(int64_t)(k + 1) * lda + k];
+      const double alpha = df_to_double(Af[(int64_t)(k + 1) * lda + k]);
       if (s2 == 0.0) {
         s_skip = 1;
         s_tau = 0.0;
@@ -169,42 +181,58 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
         e[k] = beta;
       }
       tau[k] = s_tau;
-      d[k] = A[(int64_t)k * lda + k];
+      d[k] = df_to_double(Af[(int64_t)k * lda + k]);
     }
     __syncthreads();
     if (s_skip) continue;
-    // v: v[k+1] = 1, v[i] = A[i][k] * s_beta, stored in column k and, for a
-    // contiguous copy read by the back-transformation, in row k (row and
-    // column k are not touched by the later steps)
+    // v: v[k+1] = 1, v[i] = A[i][k] * s_beta, stored (FP64) in column k and,
+    // for a contiguous copy read by the back-transformation, in row k (row
+    // and column k are not touched by the later steps)
     const int m0 = k + 1;
     double* vs = svec;
     double* ws = svec + lda;
+    float2* vsf = reinterpret_cast<float2*>(svec + 2 * lda);
+    float2* wsf = reinterpret_cast<float2*>(svec + 3 * lda);
     for (int i = m0 + t; i < n; i += kEigThreads) {
       double vi;
       if (i == m0) vi = 1.0;
       else {
-        vi = A[(int64_t)i * lda + k] * s_beta;
+        vi = df_to_double(Af[(int64_t)i * lda + k]) * s_beta;
         A[(int64_t)i * lda + k] = vi;
       }
       A[(int64_t)k * lda + i] = vi;
       vs[i] = vi;
+      vsf[i] = df_split(vi);
     }
     __syncthreads();
     // p = tau * A22 v: warp per row (A22 is kept symmetric, so row i is
-    // column i), lanes along the row, two rows in flight per warp
+    // column i), lanes along the row, two rows in flight per warp; the row
+    // sums in double-float, reduced over the warp with the two-sum
     double pdot = 0.0;
     for (int i = m0 + warp_e; i < n; i += 2 * nwarp_e) {
       const int i2 = i + nwarp_e;
-      const double* Ai = A + (int64_t)i * lda;
-      const double* Ai2 = A + (int64_t)(i2 < n ? i2 : i) * lda;
-      double a1 = 0.0, a2 = 0.0;
+      const float2* Ai = Af + (int64_t)i * lda;
+      const float2* Ai2 = Af + (int64_t)(i2 < n ? i2 : i) * lda;
+      float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
       for (int j = m0 + lane_e; j < n; j += 32) {
-        const double vj = vs[j];
-        a1 = fma(Ai[j], vj, a1);
-        a2 = fma(Ai2[j], vj, a2);
+        const float2 vj = vsf[j];
+        df_fma(Ai[j], vj, h1, l1);
+        df_fma(Ai2[j], vj, h2, l2);
       }
-      a1 = warp_sum(a1) * s_tau;
-      a2 = warp_sum(a2) * s_tau;
+      {
+        float h = __fadd_rn(h1, l1), l = __fsub_rn(l1, __fsub_rn(h, h1));
+        float g = __fadd_rn(h2, l2), m = __fsub_rn(l2, __fsub_rn(g, h2));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float bh = __shfl_xor_sync(0xffffffffu, h, o), bl = __shfl_xor_sync(0xffffffffu, l, o);
+          const float ch = __shfl_xor_sync(0xffffffffu, g, o), cl = __shfl_xor_sync(0xffffffffu, m, o);
+          df_add(h, l, bh, bl);
+          df_add(g, m, ch, cl);
+        }
+        h1 = h; l1 = l; h2 = g; l2 = m;
+      }
+      const double a1 = ((double)h1 + (double)l1) * s_tau;
+      const double a2 = ((double)h2 + (double)l2) * s_tau;
       if (lane_e == 0) {
         ws[i] = a1;
         pdot += a1 * vs[i];
@@ -217,23 +245,34 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
     pdot = block_sum(pdot, sh);
     if (t == 0) s_K = -0.5 * s_tau * pdot;
     __syncthreads();
-    for (int i = m0 + t; i < n; i += kEigThreads) ws[i] += s_K * vs[i];  // w
+    for (int i = m0 + t; i < n; i += kEigThreads) {  // w
+      const double wi = ws[i] + s_K * vs[i];
+      ws[i] = wi;
+      wsf[i] = df_split(wi);
+    }
     __syncthreads();
-    // A22 -= v w' + w v': warp per row, lanes along the row
+    // A22 -= v w' + w v' in double-float: warp per row, lanes along the row
     for (int i = m0 + warp_e; i < n; i += nwarp_e) {
-      double* Ai = A + (int64_t)i * lda;
-      const double vi = vs[i], wi = ws[i];
-      for (int j = m0 + lane_e; j < n; j += 32) Ai[j] -= vs[j] * wi + ws[j] * vi;
+      float2* Ai = Af + (int64_t)i * lda;
+      const float2 vi = vsf[i], wi = wsf[i];
+      for (int j = m0 + lane_e; j < n; j += 32) {
+        float uh = 0.f, ul = 0.f;
+        df_fma(vsf[j], wi, uh, ul);
+        df_fma(wsf[j], vi, uh, ul);
+        float2 a = Ai[j];
+        df_add(a.x, a.y, -uh, -ul);
+        Ai[j] = a;
+      }
     }
     __syncthreads();
   }
   if (t == 0) {
     if (n >= 2) {
-      d[n - 2] = A[(int64_t)(n - 2) * lda + (n - 2)];
-      e[n - 2] = A[(int64_t)(n - 1) * lda + (n - 2)];
+      d[n - 2] = df_to_double(Af[(int64_t)(n - 2) * lda + (n - 2)]);
+      e[n - 2] = df_to_double(Af[(int64_t)(n - 1) * lda + (n - 2)]);
       tau[n - 2] = 0.0;
     }
-    d[n - 1] = A[(int64_t)(n - 1) * lda + (n - 1)];
+    d[n - 1] = df_to_double(Af[(int64_t)(n - 1) * lda + (n - 1)]);
     if (n >= 1) e[n - 1] = 0.0;
   }
   __syncthreads();
@@ -420,9 +459,9 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* Aall, int 
 int sym_eig_top(int nmat, double* A, int lda, const int32_t* nsize, int want, double* theta,
                 double* S, double* work, const int32_t* active, cudaStream_t stream) {
   if (nmat <= 0) return LAPY_OK;
-  // v and w of a reflector (2 lda), partial dots of the back-transformation
-  // (5 want)
-  const size_t smem = sizeof(double) * std::max<size_t>(2 * (size_t)lda, 5 * (size_t)want);
+  // v and w of a reflector in FP64 and double-float (4 lda), partial dots of
+  // the back-transformation (5 want)
+  const size_t smem = sizeof(double) * std::max<size_t>(4 * (size_t)lda, 5 * (size_t)want);
   if (smem > 48 * 1024) {
     LAPY_CUDA_TRY(cudaFuncSetAttribute(sym_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <vector>
 #include "blas.cuh"
+#include "dfloat.cuh"
 #include "dense.cuh"
 #include "solve.cuh"
 #include "coarse.cuh"
@@ -233,34 +234,6 @@ __global__ void to_df_inplace_kernel(int64_t m, double* x) {
   const double v = x[i];
   const float h = __double2float_rn(v);
   reinterpret_cast<float2*>(x)[i] = make_float2(h, __double2float_rn(v - (double)h));
-}
-
-__device__ __forceinline__ float2 df_split(double v) {
-  const float h = __double2float_rn(v);
-  return make_float2(h, __double2float_rn(v - (double)h));
-}
-
-// (h, l) += (bh, bl), renormalised; commutative, so a butterfly of these
-// leaves the same sum in every lane
-__device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
-  const float s = __fadd_rn(h, bh);
-  const float v = __fsub_rn(s, h);
-  const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, v)), __fsub_rn(bh, v));
-  const float t = __fadd_rn(__fadd_rn(l, bl), e);
-  h = __fadd_rn(s, t);
-  l = __fsub_rn(t, __fsub_rn(h, s));
-}
-
-__device__ __forceinline__ void df_fma(float2 x, float2 y, float& sh, float& sl) {
-  const float p = __fmul_rn(x.x, y.x);
-  float e = fmaf(x.x, y.x, -p);
-  e = fmaf(x.x, y.y, e);
-  e = fmaf(x.y, y.x, e);
-  const float t = __fadd_rn(sh, p);
-  const float v = __fsub_rn(t, sh);
-  const float r = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, v)), __fsub_rn(p, v));
-  sl = __fadd_rn(sl, __fadd_rn(r, e));
-  sh = t;
 }
 
 // TN with the basis in double-float form (see gemm_tn_blk_kernel for the layout).
