@@ -37,7 +37,7 @@ import numpy as np
 DEFAULT = {"block": 4, "agg_target": 64, "round_rtol": 1e-3, "ctas_per_sm": 5}
 CANDIDATES = {
     "block": [4, 2, 8],
-    "agg_target": [64, 96],
+    "agg_target": [64, 96, 48],
     "round_rtol": [1e-3, 3e-3],
     "ctas_per_sm": [5, 4],
 }
