@@ -422,33 +422,55 @@ __global__ void __launch_bounds__(kEigThreads, 4) sym_eig_kernel(double* Aall, i
 
   // ---- 4. back-transformation Y <- H_0 ... H_{n-3} Y, one reflector at a
   // time for all vectors (the reflector is read from its copy in row k):
-  // column dots by (row part, vector) threads, then the rank-1 update
+  // column dots by (row part, vector) threads, then the rank-1 update.  Y is
+  // held in double-float meanwhile (its O(n^2 nw) products run on the FP32
+  // pipe); each reflector is split once into shared memory.
   constexpr int kBtCols = 64, kBtRows = kEigThreads / kBtCols;
   const int tx = t % kBtCols, ty = t / kBtCols;
-  double* part = svec;                      // kBtRows x want partial dots
-  double* dps = svec + (int64_t)kBtRows * want;  // want scaled dots
+  float2* part = reinterpret_cast<float2*>(svec);                 // kBtRows x want partial dots
+  double* dps = svec + (int64_t)kBtRows * want;                   // want scaled dots
+  float2* dpsf = reinterpret_cast<float2*>(dps + want);           // the same, double-float
+  float2* vkf = reinterpret_cast<float2*>(dps + 2 * (int64_t)want);  // the reflector, double-float (lda)
+  float2* Yf = reinterpret_cast<float2*>(Y);
+  for (int i = ty; i < n; i += kBtRows)
+    for (int q = tx; q < nw; q += kBtCols) Yf[(int64_t)i * want + q] = df_split(Y[(int64_t)i * want + q]);
+  __syncthreads();
   for (int k = n - 3; k >= 0; --k) {
     const double tk = tau[k];
     if (tk == 0.0) continue;  // uniform: tau is in global memory, read by all
     const double* vk = A + (int64_t)k * lda;  // vk[k+1] = 1
+    for (int i = k + 1 + t; i < n; i += kEigThreads) vkf[i] = df_split(vk[i]);
+    __syncthreads();
     for (int q = tx; q < nw; q += kBtCols) {
-      double acc = 0.0;
-      for (int i = k + 1 + ty; i < n; i += kBtRows) acc = fma(vk[i], Y[(int64_t)i * want + q], acc);
-      part[ty * want + q] = acc;
+      float h = 0.f, l = 0.f;
+      for (int i = k + 1 + ty; i < n; i += kBtRows) df_fma(vkf[i], Yf[(int64_t)i * want + q], h, l);
+      const float hh = __fadd_rn(h, l);
+      part[ty * want + q] = make_float2(hh, __fsub_rn(l, __fsub_rn(hh, h)));
     }
     __syncthreads();
     for (int q = t; q < nw; q += kEigThreads) {
-      double s = 0.0;
-      for (int r = 0; r < kBtRows; ++r) s += part[r * want + q];
-      dps[q] = tk * s;
+      float h = 0.f, l = 0.f;
+      for (int r = 0; r < kBtRows; ++r) df_add(h, l, part[r * want + q].x, part[r * want + q].y);
+      const double d = tk * ((double)h + (double)l);
+      dps[q] = d;
+      dpsf[q] = df_split(d);
     }
     __syncthreads();
     for (int i = k + 1 + ty; i < n; i += kBtRows) {
-      const double vi = vk[i];
-      for (int q = tx; q < nw; q += kBtCols) Y[(int64_t)i * want + q] -= dps[q] * vi;
+      const float2 vi = vkf[i];
+      for (int q = tx; q < nw; q += kBtCols) {
+        float uh = 0.f, ul = 0.f;
+        df_fma(dpsf[q], vi, uh, ul);
+        float2 y = Yf[(int64_t)i * want + q];
+        df_add(y.x, y.y, -uh, -ul);
+        Yf[(int64_t)i * want + q] = y;
+      }
     }
     __syncthreads();
   }
+  for (int i = ty; i < n; i += kBtRows)
+    for (int q = tx; q < nw; q += kBtCols) Y[(int64_t)i * want + q] = df_to_double(Yf[(int64_t)i * want + q]);
+  __syncthreads();
   // rows beyond n and columns beyond nw (if want > n) are zero
   for (int i = ty; i < lda; i += kBtRows)
     for (int q = tx; q < want; q += kBtCols)
@@ -459,9 +481,10 @@ __global__ void __launch_bounds__(kEigThreads, 4) sym_eig_kernel(double* Aall, i
 int sym_eig_top(int nmat, double* A, int lda, const int32_t* nsize, int want, double* theta,
                 double* S, double* work, const int32_t* active, cudaStream_t stream) {
   if (nmat <= 0) return LAPY_OK;
-  // v and w of a reflector in FP64 and double-float (4 lda), partial dots of
-  // the back-transformation (5 want)
-  const size_t smem = sizeof(double) * std::max<size_t>(4 * (size_t)lda, 5 * (size_t)want);
+  // v and w of a reflector in FP64 and double-float (4 lda); partial dots,
+  // scaled dots and the double-float reflector of the back-transformation
+  // (6 want + lda)
+  const size_t smem = sizeof(double) * std::max<size_t>(4 * (size_t)lda, 6 * (size_t)want + (size_t)lda);
   if (smem > 48 * 1024) {
     LAPY_CUDA_TRY(cudaFuncSetAttribute(sym_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
