@@ -272,9 +272,8 @@ int lapy_pcg_solve(int64_t n, const int32_t* indptr, const int32_t* indices,
  * scratch is a static device array of LAPY_STATIC_SCRATCH_BYTES that every
  * GPU loading the library holds until exit.  Problems needing more scratch
  * (lapy_pcg_solve_workspace_bytes) are rejected with LAPY_ERR_WORKSPACE.  The
- * first call on a device looks up the array's address (cudaGetSymbolAddress)
- * and should come before any stream capture; the address is kept for the
- * life of the process, so the entry point must not be used on a device after
+ * first call on a device looks up the array's address (cudaGetSymbolAddress);
+ * the address is kept for the life of the process, so the entry point must not be used on a device after
  * a cudaDeviceReset of it.  Like lapy_pcg_solve it returns once the solve has
  * finished on `stream`.  All calls share the array and each leaves its
  * contents behind: calls that overlap on the GPU (two streams or two host

@@ -499,8 +499,7 @@ extern "C" int lapy_ic0_pcg_solve(int64_t n, const int32_t* indptr, const int32_
 // workspace.  Its scratch is this file-scope device array (held by every GPU
 // that loads the library, until the process exits); its address is looked up
 // once per device with cudaGetSymbolAddress, on the first call made with that
-// device current, so that first call should come before any stream capture.
-// The looked-up address is kept for the life of the process: after a
+// device current.  The looked-up address is kept for the life of the process: after a
 // cudaDeviceReset of a device, this entry point must not be called on it
 // again (the module is reloaded and the kept address is stale).  Like
 // lapy_pcg_solve, the call returns after the solve has finished on `stream`.
