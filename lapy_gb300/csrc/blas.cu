@@ -17,22 +17,24 @@ __global__ void seg_col_norm2_kernel(const double* __restrict__ x, const double*
   }
 }
 
-// Per-chunk column sums of x .* y (NC columns, one CTA per chunk, every
-// thread accumulating all columns of its rows), then per segment the sum of
+// Per-chunk column sums of x .* y (NC columns, one warp per chunk, every
+// lane accumulating all columns of its rows), then per segment the sum of
 // its chunks' partials in chunk order: reproducible, and a large segment is
 // spread over many CTAs instead of one.
 template <int NC>
 __global__ void __launch_bounds__(256) chunk_col_dot_kernel(const double* __restrict__ x, const double* __restrict__ y,
-                                                            const int32_t* __restrict__ chunk_row,
+                                                            int nchunk, const int32_t* __restrict__ chunk_row,
                                                             double* __restrict__ part) {
-  __shared__ double sh[NC][8];
-  const int c = blockIdx.x;
+  // one warp per chunk (no block barrier): lanes stride the chunk's rows
+  const int c = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= nchunk) return;
   const int64_t r0 = chunk_row[c], r1 = chunk_row[c + 1];
   double acc[NC];
 #pragma unroll
   for (int q = 0; q < NC; ++q) acc[q] = 0.0;
-#pragma unroll 2
-  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+#pragma unroll 4
+  for (int64_t r = r0 + lane; r < r1; r += 32) {
     const double* xr = x + r * NC;
     const double* yr = y + r * NC;
     if constexpr (NC % 2 == 0) {
@@ -47,18 +49,10 @@ __global__ void __launch_bounds__(256) chunk_col_dot_kernel(const double* __rest
       acc[0] += xr[0] * yr[0];
     }
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
     const double v = warp_sum(acc[q]);
-    if (lane == 0) sh[q][warp] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < NC) {
-    double t = 0.0;
-#pragma unroll
-    for (int w = 0; w < 8; ++w) t += sh[threadIdx.x][w];
-    part[(int64_t)c * kChunkScratch + threadIdx.x] = t;
+    if (lane == q) part[(int64_t)c * kChunkScratch + q] = v;
   }
 }
 
@@ -78,7 +72,8 @@ __global__ void seg_sum_chunks_kernel(int nseg, int ncol, const int32_t* __restr
 
 template <int NC>
 static int chunked_dot(const double* x, const double* y, const ChunkTable& ct, double* out, cudaStream_t stream) {
-  chunk_col_dot_kernel<NC><<<ct.nchunk, 256, 0, stream>>>(x, y, ct.chunk_row, ct.scratch);
+  chunk_col_dot_kernel<NC><<<lapy_ceil_div((int64_t)ct.nchunk * 32, 256), 256, 0, stream>>>(x, y, ct.nchunk,
+                                                                                           ct.chunk_row, ct.scratch);
   LAPY_TRY(lapy_check_launch("chunk_col_dot_kernel"));
   seg_sum_chunks_kernel<<<lapy_ceil_div((int64_t)ct.nseg * NC * 32, 128), 128, 0, stream>>>(ct.nseg, NC, ct.seg_chunk,
                                                                                            ct.scratch, out);

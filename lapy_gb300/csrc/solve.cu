@@ -41,10 +41,13 @@ __global__ void mask_cols_kernel(float* __restrict__ R, int p, const int32_t* __
 }
 
 // R -= K X in FP64 (R holds B on entry): the SELL copy when present.
-static int residual64(const SysMatrix& K, const ChunkTable& ct, int p, const double* X, double* R, int G,
-                      cudaStream_t stream) {
-  if (K.sell64.val && sell_spmm<double>(K.sell64, ct.nunit, ct.unit_row, p, X, R, -1.0, 1.0, stream) == LAPY_OK)
+// R = B - K X in FP64 (from the SELL copy in one pass; else B copied, then
+// the CSR product subtracted)
+static int residual64(const SysMatrix& K, const ChunkTable& ct, int p, const double* X, const double* B, double* R,
+                      int G, cudaStream_t stream) {
+  if (K.sell64.val && sell_spmm<double>(K.sell64, ct.nunit, ct.unit_row, p, X, R, -1.0, 1.0, stream, B) == LAPY_OK)
     return LAPY_OK;
+  LAPY_CUDA_TRY(cudaMemcpyAsync(R, B, sizeof(double) * K.n * p, cudaMemcpyDeviceToDevice, stream));
   return csr_spmm<double>(K.n, K.indptr, K.indices, K.k64, p, X, R, -1.0, 1.0, G, stream);
 }
 
@@ -83,8 +86,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
     local.rounds = 1;
     local.pcg_iters = it;
     LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));
-    LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
-    LAPY_TRY(residual64(K, ct, p, X, R64, G, stream));
+    LAPY_TRY(residual64(K, ct, p, X, B, R64, G, stream));
     LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
     LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
     LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -102,8 +104,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
     local.rounds = 1;
     local.pcg_iters = it;
     LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));
-    LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
-    LAPY_TRY(residual64(K, ct, p, X, R64, G, stream));
+    LAPY_TRY(residual64(K, ct, p, X, B, R64, G, stream));
     LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
     LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
     LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -136,8 +137,7 @@ int ir_solve(const SysMatrix& K, const ChunkTable& ct, int p, const double* B, d
       local.rounds++;
       local.pcg_iters += it;
       LAPY_TRY(add_f32_to_f64(n * p, D32, X, stream));
-      LAPY_CUDA_TRY(cudaMemcpyAsync(R64, B, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, stream));
-      LAPY_TRY(residual64(K, ct, p, X, R64, G, stream));
+      LAPY_TRY(residual64(K, ct, p, X, B, R64, G, stream));
       LAPY_TRY(seg_col_norm2(R64, p, ct, rn2, stream));
       LAPY_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
       LAPY_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(int32_t) * nsp, cudaMemcpyDeviceToHost, stream));

@@ -84,7 +84,8 @@ template <typename V, int NP>
 __global__ void __launch_bounds__(256) sell_spmm_kernel(int nunit, const int32_t* __restrict__ unit_row,
                                                         const int32_t* __restrict__ slice_ptr,
                                                         const int32_t* __restrict__ col, const V* __restrict__ val,
-                                                        const V* __restrict__ x, V* __restrict__ y, V alpha, V beta) {
+                                                        const V* __restrict__ x, const V* __restrict__ b,
+                                                        V* __restrict__ y, V alpha, V beta) {
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunit; u += nw) {
@@ -103,20 +104,21 @@ __global__ void __launch_bounds__(256) sell_spmm_kernel(int nunit, const int32_t
     const int64_t row = unit_row[u] + lane;
     if (row < unit_row[u + 1]) {
       V* yr = y + row * NP;
+      const V* br = b ? b + row * NP : yr;  // y = alpha A x + beta b (b = y when null)
 #pragma unroll
-      for (int q = 0; q < NP; ++q) yr[q] = (beta == V(0)) ? alpha * acc[q] : alpha * acc[q] + beta * yr[q];
+      for (int q = 0; q < NP; ++q) yr[q] = (beta == V(0)) ? alpha * acc[q] : alpha * acc[q] + beta * br[q];
     }
   }
 }
 
 template <typename V>
 int sell_spmm(const SellMatrix<V>& M, int nunit, const int32_t* unit_row, int ncol, const V* x, V* y, V alpha,
-              V beta, cudaStream_t stream) {
+              V beta, cudaStream_t stream, const V* b) {
   if (!M.val || nunit <= 0) return LAPY_ERR_INVALID;
   const unsigned grid = std::min<unsigned>(lapy_ceil_div((int64_t)nunit * 32, 256), 8u * lapy_num_sms());
 #define LAPY_SELL_CASE(NPV)                                                                                  \
   case NPV:                                                                                                \
-    sell_spmm_kernel<V, NPV><<<grid, 256, 0, stream>>>(nunit, unit_row, M.slice_ptr, M.col, M.val, x, y, alpha, \
+    sell_spmm_kernel<V, NPV><<<grid, 256, 0, stream>>>(nunit, unit_row, M.slice_ptr, M.col, M.val, x, b, y, alpha, \
                                                        beta);                                              \
     return lapy_check_launch("sell_spmm_kernel");
   switch (ncol) {
@@ -132,9 +134,9 @@ int sell_spmm(const SellMatrix<V>& M, int nunit, const int32_t* unit_row, int nc
 }
 
 template int sell_spmm<double>(const SellMatrix<double>&, int, const int32_t*, int, const double*, double*, double,
-                               double, cudaStream_t);
+                               double, cudaStream_t, const double*);
 template int sell_spmm<float>(const SellMatrix<float>&, int, const int32_t*, int, const float*, float*, float, float,
-                              cudaStream_t);
+                              cudaStream_t, const float*);
 
 }  // namespace lapy
 

@@ -39,11 +39,11 @@ __device__ __forceinline__ void row_dot_group(const int32_t* __restrict__ indptr
   }
 }
 
-// Y = alpha * Mat * X + beta * Y from a SELL copy (one warp per 32-row unit,
-// lane = row; ncol in {1, 2, 4, 8, 16}).  Returns LAPY_ERR_INVALID for other
-// widths (callers then use csr_spmm).
+// Y = alpha * Mat * X + beta * B from a SELL copy (B = Y when null; one warp
+// per 32-row unit, lane = row; ncol in {1, 2, 4, 8, 16}).  Returns
+// LAPY_ERR_INVALID for other widths (callers then use csr_spmm).
 template <typename V>
 int sell_spmm(const SellMatrix<V>& M, int nunit, const int32_t* unit_row, int ncol, const V* x, V* y, V alpha,
-              V beta, cudaStream_t stream);
+              V beta, cudaStream_t stream, const V* b = nullptr);
 
 }  // namespace lapy
