@@ -51,10 +51,45 @@ static int launch_spmm_g(int64_t n, const int32_t* indptr, const int32_t* indice
   return lapy_check_launch("spmm_kernel");
 }
 
+// Many columns (ncol > 8, e.g. the final Rayleigh-Ritz block): one thread per
+// (row, group of 8 columns), the row's entries walked once per group with
+// eight accumulators, so each gathered row of X is read 8 values at a time
+// (groups of lanes per row reduced through shuffles cost more here).
+template <typename V>
+__global__ void __launch_bounds__(256) spmm_rowcols_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                                                           const int32_t* __restrict__ indices,
+                                                           const V* __restrict__ vals, int ncol,
+                                                           const V* __restrict__ x, V* __restrict__ y, V alpha,
+                                                           V beta) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const int c0 = blockIdx.y * 8;
+  const int nc = min(8, ncol - c0);
+  V acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = V(0);
+  for (int32_t k = indptr[row]; k < indptr[row + 1]; ++k) {
+    const V a = __ldg(vals + k);
+    const V* xr = x + (int64_t)__ldg(indices + k) * ncol + c0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (q < nc) acc[q] += a * __ldg(xr + q);
+  }
+  V* yr = y + row * ncol + c0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    if (q < nc) yr[q] = (beta == V(0)) ? alpha * acc[q] : alpha * acc[q] + beta * yr[q];
+}
+
 template <typename V>
 int csr_spmm(int64_t n, const int32_t* indptr, const int32_t* indices, const V* vals, int ncol,
              const V* x, V* y, V alpha, V beta, int group, cudaStream_t stream) {
   if (n <= 0 || ncol <= 0) return LAPY_OK;
+  if (ncol > 8) {
+    spmm_rowcols_kernel<V><<<dim3(lapy_ceil_div(n, 256), lapy_ceil_div(ncol, 8)), 256, 0, stream>>>(
+        n, indptr, indices, vals, ncol, x, y, alpha, beta);
+    return lapy_check_launch("spmm_rowcols_kernel");
+  }
   switch (group) {
     case 4: return launch_spmm_g<V, 4>(n, indptr, indices, vals, ncol, x, y, alpha, beta, stream);
     case 8: return launch_spmm_g<V, 8>(n, indptr, indices, vals, ncol, x, y, alpha, beta, stream);
