@@ -332,9 +332,10 @@ __global__ void __launch_bounds__(256) gemm_nn_df_kernel(const float2* __restric
   }
 }
 
-// Final Rayleigh-Ritz products in double-float (one thread per output entry):
-// Y(row, b) = sum_a Q(row, a) H_s[a][b] with Q the double-float basis (blocks
-// of p columns) and H_s pre-split, ...
+// Y(row, b) = sum_a Q(row, a) H_s[a][b] in double-float, one thread per
+// output entry (Q: double-float, blocks of p columns; H_s pre-split): the
+// fallback of the register-tiled form below when H's column tile does not fit
+// in shared memory.
 __global__ void __launch_bounds__(256) gemm_nn_dfany_kernel(const float2* __restrict__ X, int p, int64_t bst,
                                                             int na, const float2* __restrict__ H,
                                                             int64_t h_seg_stride, int ldh, double* __restrict__ Y,
@@ -356,23 +357,8 @@ __global__ void __launch_bounds__(256) gemm_nn_dfany_kernel(const float2* __rest
   }
 }
 
-// ... and partial[c][a][b] = sum over chunk c's rows of X(row, a) Y(row, b)
-// for row-major double-float X (n x na) and Y (n x nb).
-__global__ void __launch_bounds__(256) gemm_tn_dfany_kernel(const float2* __restrict__ X, int na,
-                                                            const float2* __restrict__ Y, int nb,
-                                                            const int32_t* __restrict__ chunk_row,
-                                                            double* __restrict__ partial) {
-  const int c = blockIdx.x;
-  const int a = blockIdx.y * kTile + threadIdx.x / kTile;
-  const int b = blockIdx.z * kTile + threadIdx.x % kTile;
-  if (a >= na || b >= nb) return;
-  float sh = 0.f, sl = 0.f;
-  const int64_t r1 = chunk_row[c + 1];
-  for (int64_t r = chunk_row[c]; r < r1; ++r) df_fma(X[r * na + a], Y[r * nb + b], sh, sl);
-  partial[((int64_t)c * na + a) * nb + b] = (double)sh + (double)sl;
-}
 
-// Register-tiled forms of the two products above.
+// Register-tiled forms of the final Rayleigh-Ritz products.
 //
 // NN: Y(row, b0 + t) = sum_a X(row, a) H_s[a][b0 + t], t < TB, for a
 // double-float X stored as blocks of bs columns (block stride bst float2;
