@@ -127,6 +127,25 @@ def solver_tuning(choice: dict) -> dict:
     return {k: v for k, v in choice.items() if k in SOLVER_KEYS}
 
 
+def timed_trial(fem, k: int, choice: dict, repeats: int = 1, sync=lambda: None) -> float:
+    """Median seconds of `repeats` eigensolves of `fem` with the knobs of
+    `choice`; inf when a solve fails or the solver rejects a knob value (such
+    a choice is never kept)."""
+    times = []
+    for _ in range(repeats):
+        sync()
+        t0 = time.perf_counter()
+        try:
+            _, _, info = fem.eigs(k=k, block=int(choice["block"]), tuning=solver_tuning(choice))
+        except ValueError:
+            return float("inf")
+        sync()
+        if any(int(s) != 0 for s in info["status"]):
+            return float("inf")
+        times.append(time.perf_counter() - t0)
+    return float(np.median(times))
+
+
 def calibrate(meshes, k: int = 50, sample: int = 32, candidates: dict | None = None, cache: TuneCache | None = None,
               repeats: int = 1) -> tuple[dict, list]:
     """Time the candidates on a stratified sample of `meshes` and store the
@@ -140,22 +159,8 @@ def calibrate(meshes, k: int = 50, sample: int = 32, candidates: dict | None = N
     fem = BatchedFEM.from_input(BatchInput([meshes[i] for i in idx]), lump=False)
     fem.eigs(k=k, block=DEFAULT["block"], tuning=solver_tuning(DEFAULT))  # warm-up
 
-    def measure(choice):
-        times = []
-        for _ in range(repeats):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            try:
-                _, _, info = fem.eigs(k=k, block=int(choice["block"]), tuning=solver_tuning(choice))
-            except ValueError:  # a knob value the solver rejects is never chosen
-                return float("inf")
-            torch.cuda.synchronize()
-            if any(int(s) != 0 for s in info["status"]):
-                return float("inf")
-            times.append(time.perf_counter() - t0)
-        return float(np.median(times))
-
-    choice, report = descend(measure, candidates=candidates)
+    choice, report = descend(lambda c: timed_trial(fem, k, c, repeats, torch.cuda.synchronize),
+                             candidates=candidates)
     cache = cache or TuneCache()
     cache.put(device_key(), shape_class(seg, k), choice,
               [{"choice": c, "seconds": t} for c, t in report])
@@ -174,4 +179,4 @@ def choice_for(meshes_or_seg_row, k: int, cache: TuneCache | None = None) -> dic
 
 
 __all__ = ["DEFAULT", "CANDIDATES", "TuneCache", "calibrate", "choice_for", "descend", "shape_class",
-           "stratified_sample", "solver_tuning", "device_key", "cache_path"]
+           "stratified_sample", "solver_tuning", "device_key", "cache_path", "timed_trial"]

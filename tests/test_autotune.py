@@ -49,3 +49,26 @@ def test_cache_round_trip(tmp_path):
     assert again.get("other", "shape") is None
     assert autotune.solver_tuning({"block": 8, "agg_target": 96, "round_rtol": 3e-3}) == \
         {"agg_target": 96, "round_rtol": 3e-3}
+
+
+class _FakeFem:
+    """Stands for a BatchedFEM: rejects an aggregate size, fails a block width."""
+
+    def __init__(self):
+        self.calls = []
+
+    def eigs(self, k, block, tuning):
+        self.calls.append((block, dict(tuning)))
+        if tuning.get("agg_target") == 48:
+            raise ValueError("eigs_shift_invert: invalid argument (agg_target)")
+        return None, None, {"status": [0, -3] if block == 2 else [0, 0]}
+
+
+def test_timed_trial_rejected_and_failed_choices_are_infinite():
+    fem = _FakeFem()
+    assert autotune.timed_trial(fem, 50, dict(autotune.DEFAULT, agg_target=48)) == float("inf")
+    assert autotune.timed_trial(fem, 50, dict(autotune.DEFAULT, block=2)) == float("inf")
+    t = autotune.timed_trial(fem, 50, dict(autotune.DEFAULT), repeats=3)
+    assert 0.0 <= t < 1.0
+    # the solver sees only its own knobs (block goes by argument)
+    assert all("block" not in tn for _, tn in fem.calls)
