@@ -10,6 +10,7 @@
 // split into its dominant rank-1 term (FP32) and a BF16 remainder for the
 // per-iteration coarse product of the PCG.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -68,13 +69,20 @@ size_t two_level_bytes(int64_t n, const int32_t* seg_row, int nseg, int nvc) {
 
 // ---- host aggregation -------------------------------------------------------
 // Labels rows [r0, r1) with local aggregate ids 0..nc-1 (lab: global array).
+// Scratch reused across the segments one host thread aggregates (no
+// allocation per aggregate once the vectors have grown).
+struct AggScratch {
+  std::vector<int32_t> queue, parent, conn_ids, conn_cnt, remap;
+  std::vector<std::vector<int32_t>> members;
+};
+
 static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, const int32_t* indices,
-                             int32_t* lab, int agg_target) {
+                             int32_t* lab, int agg_target, AggScratch& sc) {
   const int32_t len = r1 - r0;
   if (len <= 0) return 0;
   const int target = seg_target(len, agg_target);
   for (int32_t v = r0; v < r1; ++v) lab[v] = -1;
-  std::vector<int32_t> queue;
+  std::vector<int32_t>& queue = sc.queue;
   queue.reserve(target);
   int32_t id = 0;
   for (int32_t v = r0; v < r1; ++v) {
@@ -97,16 +105,19 @@ static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, cons
   }
   // merge aggregates below target / 4 rows into the neighbour aggregate
   // with the most connecting entries (ties: the smaller id)
-  std::vector<std::vector<int32_t>> members(id);
+  std::vector<std::vector<int32_t>>& members = sc.members;
+  if ((int32_t)members.size() < id) members.resize(id);
+  for (int32_t a = 0; a < id; ++a) members[a].clear();
   for (int32_t v = r0; v < r1; ++v) members[lab[v]].push_back(v);
-  std::vector<int32_t> parent(id);
+  std::vector<int32_t>& parent = sc.parent;
+  parent.resize(id);
   for (int32_t a = 0; a < id; ++a) parent[a] = a;
   auto find = [&](int32_t a) {
     while (parent[a] != a) a = parent[a] = parent[parent[a]];
     return a;
   };
-  std::vector<int32_t> conn_ids;
-  std::vector<int32_t> conn_cnt;
+  std::vector<int32_t>& conn_ids = sc.conn_ids;
+  std::vector<int32_t>& conn_cnt = sc.conn_cnt;
   for (int32_t a = 0; a < id; ++a) {
     if (parent[a] != a || (int)members[a].size() >= target / 4) continue;
     conn_ids.clear();
@@ -137,7 +148,8 @@ static int aggregate_segment(int32_t r0, int32_t r1, const int32_t* indptr, cons
     members[a].clear();
   }
   // compact: ids in order of each aggregate's first row
-  std::vector<int32_t> remap(id, -1);
+  std::vector<int32_t>& remap = sc.remap;
+  remap.assign(id, -1);
   int32_t nc = 0;
   for (int32_t v = r0; v < r1; ++v) {
     const int32_t a = find(lab[v]);
@@ -329,6 +341,19 @@ __global__ void __launch_bounds__(kInvThreads) coarse_inverse_kernel(const int32
   }
 }
 
+// Segments largest first: host threads take them from a shared counter
+// (mesh sizes differ by 64x between levels; a fixed round-robin split left
+// threads idle).  Every segment writes its own rows only, so the result does
+// not depend on which thread ran it.
+static std::vector<int32_t> largest_first(const int32_t* seg_row, int nseg) {
+  std::vector<int32_t> order(nseg);
+  for (int s = 0; s < nseg; ++s) order[s] = s;
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+    return seg_row[a + 1] - seg_row[a] > seg_row[b + 1] - seg_row[b];
+  });
+  return order;
+}
+
 static int host_threads(int nseg) {
   return std::max(1, std::min<int>(nseg, std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
 }
@@ -337,13 +362,17 @@ int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, co
                          int32_t* perm, int32_t* lab_new, int agg_target) {
   std::vector<int32_t> lab(n, -1);
   const int nthr = host_threads(nseg);
+  const std::vector<int32_t> sorder = largest_first(seg_row, nseg);
+  std::atomic<int> next{0};
   std::vector<std::thread> pool;
   for (int t = 0; t < nthr; ++t)
-    pool.emplace_back([&, t]() {
-      std::vector<int32_t> order, first, cnt, fill, agg_order, agg_rank, queue;
-      for (int s = t; s < nseg; s += nthr) {
+    pool.emplace_back([&]() {
+      std::vector<int32_t> order, first, cnt, fill, agg_order, agg_rank;
+      AggScratch sc;
+      for (int i = next.fetch_add(1); i < nseg; i = next.fetch_add(1)) {
+        const int s = sorder[i];
         const int32_t r0 = seg_row[s], r1 = seg_row[s + 1];
-        const int nc = aggregate_segment(r0, r1, hptr, hidx, lab.data(), agg_target);
+        const int nc = aggregate_segment(r0, r1, hptr, hidx, lab.data(), agg_target, sc);
         if (nc <= 0) {  // no coarse space: rows keep their order, no aggregate
           for (int32_t v = r0; v < r1; ++v) {
             perm[v] = v;
@@ -428,11 +457,17 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
     LAPY_CUDA_TRY(cudaMemcpyAsync(hidx.data(), indices, 4 * (size_t)nnz, cudaMemcpyDeviceToHost, stream));
     LAPY_CUDA_TRY(cudaStreamSynchronize(stream));
     const int nthr = host_threads(nseg);
+    const std::vector<int32_t> sorder = largest_first(seg_row, nseg);
+    std::atomic<int> next{0};
     std::vector<std::thread> pool;
     for (int t = 0; t < nthr; ++t)
-      pool.emplace_back([&, t]() {
-        for (int s = t; s < nseg; s += nthr)
-          nc[s] = aggregate_segment(seg_row[s], seg_row[s + 1], hptr.data(), hidx.data(), lab.data(), agg_target);
+      pool.emplace_back([&]() {
+        AggScratch sc;
+        for (int i = next.fetch_add(1); i < nseg; i = next.fetch_add(1)) {
+          const int s = sorder[i];
+          nc[s] = aggregate_segment(seg_row[s], seg_row[s + 1], hptr.data(), hidx.data(), lab.data(), agg_target,
+                                    sc);
+        }
       });
     for (auto& th : pool) th.join();
   }
