@@ -360,7 +360,12 @@ static int host_threads(int nseg) {
 
 int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, const int32_t* seg_row, int nseg,
                          int32_t* perm, int32_t* lab_new, int agg_target) {
-  std::vector<int32_t> lab(n, -1);
+  // labels of this call's rows (aggregate_segment sets every row of its
+  // segment); the storage is kept per calling thread across calls, like the
+  // caller's copies, and handed to the workers as a plain pointer
+  thread_local std::vector<int32_t> lab_store;
+  if ((int64_t)lab_store.size() < n) lab_store.resize(n);
+  int32_t* const lab = lab_store.data();
   const int nthr = host_threads(nseg);
   const std::vector<int32_t> sorder = largest_first(seg_row, nseg);
   std::atomic<int> next{0};
@@ -372,7 +377,7 @@ int plan_aggregate_order(int64_t n, const int32_t* hptr, const int32_t* hidx, co
       for (int i = next.fetch_add(1); i < nseg; i = next.fetch_add(1)) {
         const int s = sorder[i];
         const int32_t r0 = seg_row[s], r1 = seg_row[s + 1];
-        const int nc = aggregate_segment(r0, r1, hptr, hidx, lab.data(), agg_target, sc);
+        const int nc = aggregate_segment(r0, r1, hptr, hidx, lab, agg_target, sc);
         if (nc <= 0) {  // no coarse space: rows keep their order, no aggregate
           for (int32_t v = r0; v < r1; ++v) {
             perm[v] = v;

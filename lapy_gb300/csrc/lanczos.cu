@@ -1071,11 +1071,18 @@ static int reorder_system(const EigPlan& P, const EigPtrs& e, const int32_t** in
                           const double** a_vals, const double** m_vals, int m_is_diag, std::vector<int32_t>* lab_out,
                           cudaStream_t st) {
   const int64_t n = P.n, nnz = P.nnz;
-  std::vector<int32_t> hptr(n + 1), hidx(nnz);
+  // host copies of the pattern and the permutation, kept per host thread
+  // across calls (grown, never shrunk): a repeated solve does not allocate,
+  // zero and fault in these hundreds of megabytes again
+  thread_local std::vector<int32_t> hptr, hidx, perm, nptr;
+  if ((int64_t)hptr.size() < n + 1) hptr.resize(n + 1);
+  if ((int64_t)hidx.size() < nnz) hidx.resize(nnz);
+  if ((int64_t)perm.size() < n) perm.resize(n);
+  if ((int64_t)nptr.size() < n + 1) nptr.resize(n + 1);
   LAPY_CUDA_TRY(cudaMemcpyAsync(hptr.data(), *indptr, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, st));
   LAPY_CUDA_TRY(cudaMemcpyAsync(hidx.data(), *indices, 4 * (size_t)nnz, cudaMemcpyDeviceToHost, st));
   LAPY_CUDA_TRY(cudaStreamSynchronize(st));
-  std::vector<int32_t> perm(n), nptr(n + 1, 0);
+  nptr[0] = 0;
   lab_out->assign(n, -1);
   LAPY_TRY(plan_aggregate_order(n, hptr.data(), hidx.data(), P.ct.h_seg_row.data(), P.nseg, perm.data(),
                                 lab_out->data(), P.agg_target));
