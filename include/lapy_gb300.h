@@ -47,6 +47,16 @@ long long lapy_launch_count(void);
  * coverage).  LAPY_OK, or LAPY_ERR_INVALID with lapy_last_error() saying what
  * failed. */
 int lapy_plan_check(const int32_t* seg_row, int nseg);
+/* Host only: the aggregation and row order the batched two-level eigensolver
+ * uses (no counterpart in the reference, which factorises exactly): for a
+ * symmetric CSR pattern on the host (indptr, indices; n rows in segments
+ * seg_row[0..nseg]), connected aggregates of about agg_target rows (>= 64)
+ * per segment, numbered breadth-first over the aggregate graph; perm[i] is
+ * the original row placed at position i (rows of an aggregate contiguous,
+ * segments keep their ranges) and labels[i] its aggregate's number within
+ * its segment (-1: the segment gets no coarse space).  Deterministic. */
+int lapy_aggregate_order(int64_t n, const int32_t* indptr, const int32_t* indices, const int32_t* seg_row,
+                         int nseg, int agg_target, int32_t* perm, int32_t* labels);
 /* PCG profile: when enabled, every persistent PCG launch is timed with CUDA
  * events and its work counted.  lapy_profile_read fills up to n of
  * {pcg_ms, pcg_launches, pcg_iterations, rows_processed, nnz_processed,

@@ -100,6 +100,7 @@ _SIGNATURES = {
     "lapy_vec_axpby": (_int, [_i64, _dbl, _vp, _dbl, _vp, _vp, _vp]),
     "lapy_heat_product_f64": (_int, [_i64, _vp, _vp, _i64, _int, _int, _vp, _int, _vp, _vp]),
     "lapy_plan_check": (_int, [_vp, _int]),
+    "lapy_aggregate_order": (_int, [_i64, _vp, _vp, _vp, _int, _int, _vp, _vp]),
     "lapy_csr_add_diag": (_int, [_i64, _vp, _dbl, _vp, _vp, _vp]),
     "lapy_pcg_solve_workspace_bytes": (_sz, [_i64, _i64, _int, _vp, _int, _int]),
     "lapy_pcg_solve": (_int, [_i64, _vp, _vp, _vp, _i64, _int, _vp, _int, _vp, _vp, _dbl, _int, _int, _dbl,

@@ -679,3 +679,24 @@ int build_two_level(int64_t n, const int32_t* indptr, const int32_t* indices, co
 }
 
 }  // namespace lapy
+
+extern "C" int lapy_aggregate_order(int64_t n, const int32_t* indptr, const int32_t* indices, const int32_t* seg_row,
+                                    int nseg, int agg_target, int32_t* perm, int32_t* labels) {
+  using namespace lapy;
+  if (n < 0 || nseg < 0 || !seg_row || (n > 0 && (!indptr || !indices || !perm || !labels)) ||
+      agg_target < kAggTarget || agg_target > 1024) {
+    lapy_set_last_message("aggregate_order: invalid arguments");
+    return LAPY_ERR_INVALID;
+  }
+  if (seg_row[0] != 0 || seg_row[nseg] != n) {
+    lapy_set_last_message("aggregate_order: segment rows must span [0, n)");
+    return LAPY_ERR_INVALID;
+  }
+  for (int s = 0; s < nseg; ++s)
+    if (seg_row[s + 1] < seg_row[s]) {
+      lapy_set_last_message("aggregate_order: segment rows must not decrease");
+      return LAPY_ERR_INVALID;
+    }
+  if (n == 0) return LAPY_OK;
+  return plan_aggregate_order(n, indptr, indices, seg_row, nseg, perm, labels, agg_target);
+}
